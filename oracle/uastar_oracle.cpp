@@ -1,0 +1,559 @@
+// uastar oracle: a CPU restatement of zhou13/uastar's sequential A* solvers and
+// pattern-database generator.
+//
+// TEST INFRASTRUCTURE ONLY.  Nothing in the product links or calls this file;
+// only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load the
+// shared library built from it, and only to check or time against the GPU
+// engine.  Parity is pinned by tests/golden/ (fixtures produced by the
+// reference's own CPU solvers, built unmodified from their sources by
+// oracle/Makefile.ref) and by the checksums of the reference's PDB files.
+//
+// Every function cites the reference code it restates (paths are relative to
+// the reference project's root).  Built with -ffp-contract=off so that the
+// float arithmetic of the grid search rounds exactly like the reference's
+// (no fused multiply-add on either x86-64 or aarch64).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <functional>
+#include <queue>
+#include <unordered_map>
+#include <unordered_set>
+#include <utility>
+#include <vector>
+
+extern "C" {
+
+// ---------------------------------------------------------------- grid ----
+// src/utils.hpp:119-122 (CPU direction tables and the float sqrt(2)).
+static const float kSqrt2 = 1.4142135623731f;
+static const int kDX[8] = {1, -1, 0, 0, 1, 1, -1, -1};
+static const int kDY[8] = {0, 0, 1, -1, 1, -1, 1, -1};
+static const float kCost[8] = {1, 1, 1, 1, kSqrt2, kSqrt2, kSqrt2, kSqrt2};
+
+typedef struct {
+    int solved;              // 1 if the goal was popped, 0 if the open list emptied
+    int capped;              // 1 if max_expansions stopped the search first
+    float cost;              // reference float32 g of the goal
+    int64_t straight;        // replayed counts along the returned path
+    int64_t diagonal;
+    int64_t generated;       // globalList.size() (src/pathway/CPU-solver.cpp:128)
+    int64_t expanded;        // pops that were neither closed duplicates nor the goal
+    int64_t path_len;        // cells on the path, start and goal included
+    double solve_seconds;
+} oracle_grid_result;
+
+static inline int grid_open(const uint64_t *words, int64_t id) {
+    return (int)((words[id >> 6] >> (id & 63)) & 1ull);
+}
+
+// Restates CPUPathwaySolver::initialize/solve/getSolution
+// (src/pathway/CPU-solver.cpp:63-137) and computeFValue (:139-146).  The grid
+// is the engine's bitmap (1 = open); an open cell allows all 8 out-moves and a
+// blocked one none, which is what the reference's 0xFF/0x00 direction masks
+// mean (src/pathway/input/custom.cpp:14-26, CPU-solver.cpp:98-100).  Unlike the
+// reference, an exhausted open list returns "not solved" instead of reading
+// an empty queue (CPU-solver.cpp:84-87).
+// path_out (optional, capacity path_cap) receives the cell ids start->goal.
+int oracle_grid_astar(int H, int W, const uint64_t *words, int sx, int sy, int ex, int ey,
+                      int64_t max_expansions, int32_t *path_out, int64_t path_cap,
+                      oracle_grid_result *res) {
+    struct Node {
+        int id;
+        float dist;
+        Node *prev;
+    };
+    auto t0 = std::chrono::steady_clock::now();
+    std::memset(res, 0, sizeof(*res));
+    auto fval = [&](const Node *n) {
+        int x = n->id / W, y = n->id % W;
+        int dx = std::abs(x - ex), dy = std::abs(y - ey);
+        return n->dist + std::min(dx, dy) * kSqrt2 + std::abs(dx - dy);
+    };
+    typedef std::pair<float, Node *> Item;
+    std::priority_queue<Item, std::vector<Item>, std::greater<Item>> open;
+    std::unordered_set<int> closed;
+    std::unordered_map<int, Node *> global;
+    const int target = ex * W + ey;
+    Node *start = new Node{sx * W + sy, 0.0f, nullptr};
+    open.push(std::make_pair(fval(start), start));
+    global[start->id] = start;
+    Node *goal = nullptr;
+    int64_t expanded = 0;
+    while (!open.empty()) {
+        Node *node = nullptr;
+        bool got = false;
+        while (!open.empty()) {
+            node = open.top().second;
+            open.pop();
+            if (!closed.count(node->id)) {
+                got = true;
+                break;
+            }
+        }
+        if (!got) break;
+        closed.insert(node->id);
+        if (node->id == target) {
+            goal = node;
+            break;
+        }
+        if (max_expansions > 0 && expanded >= max_expansions) {
+            res->capped = 1;
+            break;
+        }
+        ++expanded;
+        int x = node->id / W, y = node->id % W;
+        for (int i = 0; i < 8; ++i) {
+            if (!grid_open(words, node->id)) continue;
+            int nx = x + kDX[i], ny = y + kDY[i];
+            if (0 <= nx && nx < H && 0 <= ny && ny < W) {
+                int nid = nx * W + ny;
+                float dist = node->dist + kCost[i];
+                auto it = global.find(nid);
+                if (it == global.end()) {
+                    Node *nn = new Node{nid, dist, node};
+                    global[nid] = nn;
+                    open.push(std::make_pair(fval(nn), nn));
+                } else if (dist < it->second->dist) {
+                    it->second->dist = dist;
+                    it->second->prev = node;
+                    open.push(std::make_pair(fval(it->second), it->second));
+                }
+            }
+        }
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    res->solve_seconds = std::chrono::duration<double>(t1 - t0).count();
+    res->generated = (int64_t)global.size();
+    res->expanded = expanded;
+    if (goal) {
+        res->solved = 1;
+        res->cost = goal->dist;
+        std::vector<int> path;
+        for (Node *n = goal; n; n = n->prev) path.push_back(n->id);
+        std::reverse(path.begin(), path.end());
+        res->path_len = (int64_t)path.size();
+        for (size_t i = 1; i < path.size(); ++i) {
+            int ax = path[i - 1] / W, ay = path[i - 1] % W;
+            int bx = path[i] / W, by = path[i] % W;
+            if (std::abs(ax - bx) + std::abs(ay - by) == 2)
+                res->diagonal++;
+            else
+                res->straight++;
+        }
+        if (path_out)
+            for (int64_t i = 0; i < res->path_len && i < path_cap; ++i) path_out[i] = path[i];
+    }
+    for (auto &kv : global) delete kv.second;
+    return 0;
+}
+
+// Exact-arithmetic restatement of the same search: g and h are kept as the
+// integer pair (straight, diagonal) with cost a + b*sqrt(2) and compared
+// exactly, so the returned (straight, diagonal) is the unique optimum.  Used
+// to settle any case where float32 accumulation in the reference could pick a
+// path whose exact cost differs from the optimum by less than float error.
+static inline int exact_cmp(int64_t a1, int64_t b1, int64_t a2, int64_t b2) {
+    // sign((a1-a2) + (b1-b2)*sqrt(2)) computed with integers only.
+    int64_t d = a1 - a2, e = b2 - b1;  // value = d - e*sqrt(2)
+    if (e == 0) return (d > 0) - (d < 0);
+    if (d >= 0 && e < 0) return 1;
+    if (d <= 0 && e > 0) return -1;
+    int64_t lhs = d * d, rhs = 2 * e * e;
+    int s = (lhs > rhs) - (lhs < rhs);
+    return d > 0 ? s : -s;
+}
+
+int oracle_grid_astar_exact(int H, int W, const uint64_t *words, int sx, int sy, int ex, int ey,
+                            oracle_grid_result *res) {
+    auto t0 = std::chrono::steady_clock::now();
+    std::memset(res, 0, sizeof(*res));
+    struct Key {
+        int64_t fa, fb;
+        int id;
+    };
+    struct Cmp {
+        bool operator()(const Key &p, const Key &q) const {
+            int c = exact_cmp(p.fa, p.fb, q.fa, q.fb);
+            if (c != 0) return c > 0;
+            return p.id > q.id;
+        }
+    };
+    std::priority_queue<Key, std::vector<Key>, Cmp> open;
+    std::unordered_map<int, std::pair<int64_t, int64_t>> g;
+    std::unordered_map<int, int> prev;
+    std::unordered_set<int> closed;
+    auto h = [&](int id, int64_t *ha, int64_t *hb) {
+        int x = id / W, y = id % W;
+        int dx = std::abs(x - ex), dy = std::abs(y - ey);
+        *hb = std::min(dx, dy);
+        *ha = std::abs(dx - dy);
+    };
+    const int target = ex * W + ey;
+    int s = sx * W + sy;
+    int64_t ha, hb;
+    h(s, &ha, &hb);
+    g[s] = {0, 0};
+    prev[s] = -1;
+    open.push({ha, hb, s});
+    int found = -1;
+    int64_t expanded = 0;
+    while (!open.empty()) {
+        Key k = open.top();
+        open.pop();
+        if (closed.count(k.id)) continue;
+        auto gk = g[k.id];
+        h(k.id, &ha, &hb);
+        if (gk.first + ha != k.fa || gk.second + hb != k.fb) continue;  // stale
+        closed.insert(k.id);
+        if (k.id == target) {
+            found = k.id;
+            break;
+        }
+        ++expanded;
+        if (!grid_open(words, k.id)) continue;
+        int x = k.id / W, y = k.id % W;
+        for (int i = 0; i < 8; ++i) {
+            int nx = x + kDX[i], ny = y + kDY[i];
+            if (nx < 0 || nx >= H || ny < 0 || ny >= W) continue;
+            int nid = nx * W + ny;
+            int64_t na = gk.first + (i < 4 ? 1 : 0), nb = gk.second + (i < 4 ? 0 : 1);
+            auto it = g.find(nid);
+            if (it == g.end() || exact_cmp(na, nb, it->second.first, it->second.second) < 0) {
+                g[nid] = {na, nb};
+                prev[nid] = k.id;
+                int64_t a2, b2;
+                h(nid, &a2, &b2);
+                open.push({na + a2, nb + b2, nid});
+            }
+        }
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    res->solve_seconds = std::chrono::duration<double>(t1 - t0).count();
+    res->generated = (int64_t)g.size();
+    res->expanded = expanded;
+    if (found >= 0) {
+        res->solved = 1;
+        res->straight = g[found].first;
+        res->diagonal = g[found].second;
+        res->cost = (float)((double)res->straight + (double)res->diagonal * std::sqrt(2.0));
+        int64_t n = 0;
+        for (int c = found; c >= 0; c = prev[c]) ++n;
+        res->path_len = n;
+    }
+    return 0;
+}
+
+// Float comparison with the reference's tolerance (src/utils.hpp:86-111):
+// equal within 1e-3 absolute or 200 float ULPs.
+int oracle_float_equal(float a, float b) {
+    float diff = std::fabs(a - b);
+    if (diff <= 1e-3f) return 1;
+    int32_t ia, ib;
+    std::memcpy(&ia, &a, 4);
+    std::memcpy(&ib, &b, 4);
+    if ((ia < 0) != (ib < 0)) return 0;
+    int64_t ulps = std::llabs((int64_t)ia - (int64_t)ib);
+    return ulps <= 200;
+}
+
+// -------------------------------------------------------------- puzzle ----
+// Pattern database: mixed-radix rank of a partial permutation and its inverse
+// (src/puzzle/database.cpp:8-25 for the radices, :140-163 encoding,
+// :165-199 decoding), and the FIFO breadth-first generation from the goal
+// abstraction in which a tracked tile may slide into any adjacent cell not
+// holding another tracked tile (:37-84).
+typedef struct {
+    int n;                 // board side
+    int k;                 // tracked tiles
+    int tracked[16];
+    int map[64];           // tile -> index in tracked, -1 if untracked
+    uint64_t multiple[17]; // multiple[i] = prod_{j>=i} (n*n - j), multiple[k] = 1
+    uint64_t size;
+} oracle_pattern;
+
+static void pattern_init(oracle_pattern *p, int n, const int *tracked, int k) {
+    std::memset(p, 0, sizeof(*p));
+    p->n = n;
+    p->k = k;
+    for (int i = 0; i < 64; ++i) p->map[i] = -1;
+    p->size = 1;
+    for (int i = 0; i < k; ++i) {
+        p->tracked[i] = tracked[i];
+        p->map[tracked[i]] = i;
+        p->size *= (uint64_t)(n * n - i);
+        p->multiple[i] = (uint64_t)(n * n - i);
+    }
+    p->multiple[k] = 1;
+    for (int i = k - 1; i >= 0; --i) p->multiple[i] *= p->multiple[i + 1];
+}
+
+uint64_t oracle_pattern_size(int n, const int *tracked, int k) {
+    oracle_pattern p;
+    pattern_init(&p, n, tracked, k);
+    return p.size;
+}
+
+// conf[cell] = tile (0 = empty/untracked) -> rank.
+static uint64_t pattern_encode(const oracle_pattern *p, const uint8_t *conf) {
+    int index[16], vrank[16];
+    for (int i = 0; i < p->n * p->n; ++i)
+        if (conf[i] && p->map[conf[i]] >= 0) index[p->map[conf[i]]] = i;
+    for (int i = 0; i < p->k; ++i) vrank[i] = index[i];
+    for (int i = 0; i < p->k; ++i)
+        for (int j = i + 1; j < p->k; ++j)
+            if (index[i] < index[j]) --vrank[j];
+    uint64_t code = 0;
+    for (int i = 0; i < p->k; ++i) code += (uint64_t)vrank[i] * p->multiple[i + 1];
+    return code;
+}
+
+static void pattern_decode(const oracle_pattern *p, uint64_t code, uint8_t *conf) {
+    int value[16];
+    bool used[64] = {false};
+    for (int i = 0; i < p->k; ++i) {
+        value[i] = (int)(code / p->multiple[i + 1]);
+        code %= p->multiple[i + 1];
+    }
+    for (int i = 0; i < p->k; ++i) {
+        int cnt = 0;
+        while (used[cnt]) ++cnt;
+        for (int j = 0; j < value[i]; ++j) {
+            ++cnt;
+            while (used[cnt]) ++cnt;
+        }
+        value[i] = cnt;
+        used[cnt] = true;
+    }
+    std::memset(conf, 0, (size_t)p->n * p->n);
+    for (int i = 0; i < p->k; ++i) conf[value[i]] = (uint8_t)p->tracked[i];
+}
+
+uint64_t oracle_pattern_encode(int n, const int *tracked, int k, const uint8_t *conf) {
+    oracle_pattern p;
+    pattern_init(&p, n, tracked, k);
+    return pattern_encode(&p, conf);
+}
+
+void oracle_pattern_decode(int n, const int *tracked, int k, uint64_t code, uint8_t *conf) {
+    oracle_pattern p;
+    pattern_init(&p, n, tracked, k);
+    pattern_decode(&p, code, conf);
+}
+
+// Fills out[size] with BFS distances (0xFF never happens for a connected
+// abstraction).  Returns the number of states reached.
+uint64_t oracle_pdb_build(int n, const int *tracked, int k, uint8_t *out) {
+    // src/utils.hpp:120-121: the first four entries of DX/DY are the 4-moves.
+    oracle_pattern p;
+    pattern_init(&p, n, tracked, k);
+    uint8_t conf[64];
+    std::vector<bool> visited(p.size, false);
+    std::memset(out, 0xFF, p.size);
+    std::memset(conf, 0, sizeof conf);
+    for (int i = 0; i < k; ++i) conf[tracked[i] - 1] = (uint8_t)tracked[i];
+    std::queue<uint64_t> q;
+    uint64_t code = pattern_encode(&p, conf);
+    q.push(code);
+    out[code] = 0;
+    visited[code] = true;
+    uint64_t count = 1;
+    while (!q.empty()) {
+        uint64_t c = q.front();
+        q.pop();
+        pattern_decode(&p, c, conf);
+        for (int x = 0; x < n; ++x)
+            for (int y = 0; y < n; ++y) {
+                int id = x * n + y;
+                if (!conf[id]) continue;
+                for (int d = 0; d < 4; ++d) {
+                    int nx = x + kDX[d], ny = y + kDY[d];
+                    if (nx < 0 || nx >= n || ny < 0 || ny >= n) continue;
+                    int nid = nx * n + ny;
+                    if (conf[nid]) continue;
+                    std::swap(conf[id], conf[nid]);
+                    uint64_t nc = pattern_encode(&p, conf);
+                    if (!visited[nc]) {
+                        visited[nc] = true;
+                        q.push(nc);
+                        out[nc] = (uint8_t)(out[c] + 1);
+                        ++count;
+                    }
+                    std::swap(conf[id], conf[nid]);
+                }
+            }
+    }
+    return count;
+}
+
+typedef struct {
+    int solved;
+    int capped;
+    int steps;               // optimal move count (fValue of the goal)
+    int64_t stored;          // closeList.size(): states ever generated
+    int64_t expanded;        // non-stale, non-goal pops
+    double solve_seconds;
+} oracle_puzzle_result;
+
+// The pattern partitions of CPUPuzzleSolver<N>::initialize
+// (src/puzzle/CPU-solver.hpp:43-102) for N = 3 and 4.
+int oracle_puzzle_partition(int n, int *tracked_out, int *counts_out) {
+    if (n == 3) {
+        for (int i = 0; i < 8; ++i) tracked_out[i] = i + 1;
+        counts_out[0] = 8;
+        return 1;
+    }
+    if (n == 4) {
+        static const int a[8] = {1, 2, 3, 4, 5, 6, 9, 13};
+        static const int b[7] = {7, 8, 10, 11, 12, 14, 15};
+        std::memcpy(tracked_out, a, sizeof a);
+        std::memcpy(tracked_out + 8, b, sizeof b);
+        counts_out[0] = 8;
+        counts_out[1] = 7;
+        return 2;
+    }
+    return 0;
+}
+
+// Restates CPUPuzzleSolver<N>::solve (src/puzzle/CPU-solver.hpp:154-231) with
+// its additive PDB heuristic computeHValue (:287-314) and lazy deletion of
+// heap entries whose fValue no longer matches the stored node (:162-165).
+// States are packed 4 bits per cell, cell (i,j) at bit 4*(i*n+j), the layout
+// of PuzzleStorage<3>/<4> (src/puzzle/storage.hpp:44-139; the last cell of a
+// 3x3 board is implied there and stored here, which changes no comparison).
+// pdbs[t] points at the table of pattern t, in partition order.
+// moves_out (optional, capacity moves_cap) receives blank moves 0..3 indexing
+// DX/DY (:237-262).
+int oracle_puzzle_astar(int n, const uint8_t *tiles, const uint8_t *const *pdbs,
+                        int64_t max_expansions, int32_t *moves_out, int64_t moves_cap,
+                        oracle_puzzle_result *res) {
+    auto t0 = std::chrono::steady_clock::now();
+    std::memset(res, 0, sizeof(*res));
+    int tracked[16], counts[4];
+    int npat = oracle_puzzle_partition(n, tracked, counts);
+    if (npat == 0) return -1;
+    oracle_pattern pats[4];
+    int off = 0;
+    for (int t = 0; t < npat; ++t) {
+        pattern_init(&pats[t], n, tracked + off, counts[t]);
+        off += counts[t];
+    }
+    const int nn = n * n;
+    auto pack = [&](const uint8_t *c) {
+        uint64_t s = 0;
+        for (int i = 0; i < nn; ++i) s |= (uint64_t)c[i] << (4 * i);
+        return s;
+    };
+    auto unpack = [&](uint64_t s, uint8_t *c) {
+        for (int i = 0; i < nn; ++i) c[i] = (uint8_t)((s >> (4 * i)) & 15);
+    };
+    auto hval = [&](const uint8_t *c) {
+        int h = 0;
+        uint8_t pc[64];
+        for (int t = 0; t < npat; ++t) {
+            for (int i = 0; i < nn; ++i) pc[i] = (c[i] && pats[t].map[c[i]] >= 0) ? c[i] : 0;
+            h += pdbs[t][pattern_encode(&pats[t], pc)];
+        }
+        return h;
+    };
+    struct Node {
+        uint64_t ps;
+        Node *prev;
+        int f, g;
+    };
+    struct Item {
+        int f;
+        Node *node;
+        bool operator>(const Item &r) const { return f > r.f; }
+    };
+    std::priority_queue<Item, std::vector<Item>, std::greater<Item>> open;
+    std::unordered_map<uint64_t, Node *> closed;
+    uint8_t conf[64], goalc[64];
+    for (int i = 0; i < nn; ++i) goalc[i] = (uint8_t)((i + 1) % nn);
+    const uint64_t target = pack(goalc);
+    Node *root = new Node{pack(tiles), nullptr, 0, 0};
+    root->f = hval(tiles);
+    open.push({root->f, root});
+    closed[root->ps] = root;
+    Node *found = nullptr;
+    int64_t expanded = 0;
+    while (!open.empty()) {
+        Item now;
+        bool got = false;
+        while (!open.empty()) {
+            now = open.top();
+            open.pop();
+            if (closed[now.node->ps]->f == now.f) {
+                got = true;
+                break;
+            }
+        }
+        if (!got) break;
+        Node *node = now.node;
+        if (node->ps == target) {
+            found = node;
+            break;
+        }
+        if (max_expansions > 0 && expanded >= max_expansions) {
+            res->capped = 1;
+            break;
+        }
+        ++expanded;
+        unpack(node->ps, conf);
+        int bx = 0, by = 0;
+        for (int i = 0; i < nn; ++i)
+            if (!conf[i]) {
+                bx = i / n;
+                by = i % n;
+                break;
+            }
+        for (int d = 0; d < 4; ++d) {
+            int nx = bx + kDX[d], ny = by + kDY[d];
+            if (nx < 0 || nx >= n || ny < 0 || ny >= n) continue;
+            std::swap(conf[bx * n + by], conf[nx * n + ny]);
+            Node nn_{pack(conf), node, 0, node->g + 1};
+            nn_.f = nn_.g + hval(conf);
+            auto it = closed.find(nn_.ps);
+            if (it == closed.end()) {
+                Node *ins = new Node(nn_);
+                closed[ins->ps] = ins;
+                open.push({ins->f, ins});
+            } else if (it->second->f > nn_.f) {
+                *it->second = nn_;
+                open.push({nn_.f, it->second});
+            }
+            std::swap(conf[bx * n + by], conf[nx * n + ny]);
+        }
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    res->solve_seconds = std::chrono::duration<double>(t1 - t0).count();
+    res->stored = (int64_t)closed.size();
+    res->expanded = expanded;
+    if (found) {
+        res->solved = 1;
+        res->steps = found->f;
+        std::vector<int> moves;
+        for (Node *c = found; c->prev; c = c->prev) {
+            uint8_t cc[64], pc[64];
+            unpack(c->ps, cc);
+            unpack(c->prev->ps, pc);
+            int cb = 0, pb = 0;
+            for (int i = 0; i < nn; ++i) {
+                if (!cc[i]) cb = i;
+                if (!pc[i]) pb = i;
+            }
+            for (int d = 0; d < 4; ++d)
+                if (pb / n + kDX[d] == cb / n && pb % n + kDY[d] == cb % n) moves.push_back(d);
+        }
+        std::reverse(moves.begin(), moves.end());
+        if (moves_out)
+            for (size_t i = 0; i < moves.size() && (int64_t)i < moves_cap; ++i) moves_out[i] = moves[i];
+    }
+    for (auto &kv : closed) delete kv.second;
+    return 0;
+}
+
+}  // extern "C"

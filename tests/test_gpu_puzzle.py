@@ -1,0 +1,115 @@
+"""GPU pattern-database build and sliding-tile search against the reference.
+
+PDBs must equal the reference's generator byte for byte (sha256 of the
+reference's database_<n>_<tiles>.bin files); solves must return the exact
+optimal move count of the reference's CPU A*, with moves that replay to the
+goal on the host."""
+from __future__ import annotations
+
+import hashlib
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import golden
+from uastar_gb300 import Engine, EngineError
+from uastar_gb300 import _lib as L
+from uastar_gb300 import engine as E
+from uastar_gb300 import workloads as WL
+from uastar_gb300.problem import PARTITIONS, pdb_cache_names
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def peng():
+    with Engine(0) as eng:
+        eng.pdb_build(3)
+        eng.pdb_build(4)
+        yield eng
+
+
+def test_pdb3_equals_oracle_and_reference(peng):
+    t = peng.pdb_fetch(3)
+    assert (t == O.pdb_build(3, PARTITIONS[3][0])).all()
+    sums = golden("pdb_sha256.json")
+    assert hashlib.sha256(t.tobytes()).hexdigest() == sums["database_3_1_2_3_4_5_6_7_8.bin"]["sha256"]
+
+
+def test_pdb4_equals_reference_files(peng):
+    sums = golden("pdb_sha256.json")
+    t = peng.pdb_fetch(4)
+    off = 0
+    for name in pdb_cache_names(4):
+        if name not in sums:
+            pytest.skip("15-puzzle reference tables not in the fixture")
+        n = sums[name]["bytes"]
+        assert hashlib.sha256(t[off:off + n].tobytes()).hexdigest() == sums[name]["sha256"], name
+        off += n
+    assert off == t.size
+
+
+def test_pdb_load_roundtrip(peng):
+    t = peng.pdb_fetch(3)
+    with Engine(0) as e2:
+        e2.pdb_load(3, t)
+        r = e2.puzzle_solve(3, [8, 1, 3, 4, 0, 2, 7, 6, 5])
+        assert r.ok and r.steps == 14
+
+
+def test_puzzle8_golden(peng):
+    for row in golden("puzzle3_small.json"):
+        r = peng.puzzle_solve(3, row["tiles"])
+        assert r.ok and r.steps == row["ref"]["steps"], row
+        mv = peng.puzzle_moves()
+        assert len(mv) == r.steps and E.validate_puzzle_moves(3, row["tiles"], mv)
+
+
+def test_puzzle15_small_golden(peng):
+    for row in golden("puzzle4_small.json"):
+        r = peng.puzzle_solve(4, row["tiles"])
+        assert r.ok and r.steps == row["ref"]["steps"], row
+        assert E.validate_puzzle_moves(4, row["tiles"], peng.puzzle_moves())
+
+
+def test_puzzle15_x100_golden(peng):
+    rows = golden("puzzle_c3.json")
+    assert len(rows) == 100
+    for row in rows:
+        assert E.gen_puzzle(row["seed"], 4, row["walk"]).tolist() == row["tiles"]
+        r = peng.puzzle_solve(4, row["tiles"])
+        assert r.ok and r.steps == row["ref"]["steps"], row
+        assert E.validate_puzzle_moves(4, row["tiles"], peng.puzzle_moves())
+
+
+def test_puzzle15_live_oracle(peng):
+    tables = peng.pdb_fetch(4)
+    t0, t1 = tables[:518918400], tables[518918400:]
+    for seed in range(6):
+        tiles = E.gen_puzzle(seed + 500, 4, 40 + 10 * seed)
+        r = peng.puzzle_solve(4, tiles)
+        ref, _ = O.puzzle_astar(4, tiles, [t0, t1])
+        assert r.ok and ref.solved and r.steps == ref.steps
+
+
+def test_unsolvable_and_bad_boards(peng):
+    r = peng.puzzle_solve(3, [2, 1, 3, 4, 5, 6, 7, 8, 0])  # one swap: odd permutation
+    assert r.status == L.NO_SOLUTION
+    r = peng.puzzle_solve(4, [2, 1] + list(range(3, 16)) + [0])
+    assert r.status == L.NO_SOLUTION
+    with pytest.raises(EngineError):
+        peng.puzzle_solve(4, [1, 1] + list(range(3, 16)) + [0])
+    with pytest.raises(EngineError):
+        peng.puzzle_solve(5, list(range(25)))
+
+
+def test_goal_board_is_zero_moves(peng):
+    r = peng.puzzle_solve(4, list(range(1, 16)) + [0])
+    assert r.ok and r.steps == 0 and peng.puzzle_moves() == []
+
+
+def test_missing_pdb_is_reported():
+    with Engine(0) as e:
+        with pytest.raises(EngineError):
+            e.puzzle_solve(3, [8, 1, 3, 4, 0, 2, 7, 6, 5])

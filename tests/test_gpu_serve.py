@@ -1,0 +1,71 @@
+"""Serving loop (continuous batching): requests arriving while others are on
+the device are admitted as slots and memory free up; each result is the same
+alone (plain engine) and in the mix; cancellation and budget rejection are
+reported on the host."""
+from __future__ import annotations
+
+import time
+
+import pytest
+
+from uastar_gb300 import Engine
+from uastar_gb300 import _lib as L
+from uastar_gb300 import workloads as WL
+from uastar_gb300.problem import float_equal
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def seng():
+    with Engine(0) as eng:
+        eng.pdb_build(4)
+        yield eng
+
+
+def drain(eng, n, timeout=120.0):
+    got = {}
+    t0 = time.time()
+    while len(got) < n and time.time() - t0 < timeout:
+        for rid, r in eng.serve_poll():
+            got[rid] = r
+        time.sleep(0.002)
+    return got
+
+
+def test_stream_results_equal_alone_and_in_mix(seng):
+    stream = WL.serve_stream(60, rate_per_s=400.0, max_side=1024)
+    insts = [s.instance() for _, s in stream]
+    seng.serve_start(hbm_budget_gb=16.0, slots=32, rounds_per_quantum=64)
+    t0 = WL.E.now_s() + 0.05
+    ids = [seng.serve_submit(inst, t0 + dt) for (dt, _), inst in zip(stream, insts)]
+    got = drain(seng, len(ids))
+    stats = seng.serve_stop(30.0)
+    assert len(got) == len(ids)
+    assert stats["completed"] == len(ids) and stats["quanta"] > 1
+    assert stats["peak_resident"] > 1  # requests overlapped on the device
+    for rid, (dt, spec), inst in zip(ids, stream, insts):
+        r = got[rid]
+        assert r["latency_ms"] > 0
+        if isinstance(spec, WL.PuzzleSpec):
+            p = seng.puzzle_solve(4, inst.tiles)
+            assert r["status"] == L.OK and r["steps"] == p.steps
+        else:
+            p = seng.grid_solve(inst.words, spec.H, spec.W, spec.start, spec.goal)
+            assert r["status"] == p.status
+            if p.ok:
+                assert (r["straight"], r["diagonal"]) == (p.straight, p.diagonal)
+                assert float_equal(r["cost"], p.cost)
+
+
+def test_cancel_and_reject(seng):
+    seng.serve_start(hbm_budget_gb=0.5, slots=4, rounds_per_quantum=16)
+    big = WL.GridSpec(8000, 8000, 0.1, 1).instance()       # partition far above the budget
+    late = WL.PuzzleSpec(4, 200, 3).instance()
+    r_big = seng.serve_submit(big)
+    r_late = seng.serve_submit(late, WL.E.now_s() + 30.0)  # not yet arrived
+    seng.serve_cancel(r_late)
+    got = drain(seng, 2, timeout=30)
+    seng.serve_stop(10.0)
+    assert got[r_big]["status"] == L.REJECTED
+    assert got[r_late]["status"] == L.CANCELLED

@@ -1,0 +1,1177 @@
+// Batched persistent engine and continuous-batching serving loop.
+//
+// Both run GA* with one CTA per instance (a BlockTeam: the CTA's threads are
+// the instance's heaps and every round barrier is a __syncthreads), so many
+// instances of uneven size progress side by side on the 152 SMs.
+//
+//  - uastar_batch_solve: a persistent kernel whose CTAs take instances from a
+//    device work queue (largest estimate first), each with its own dedup
+//    partition in one table arena and the CTA's own heap slice; the launch
+//    sequence is captured once into a CUDA graph.  Instances that overflow
+//    their partition or heaps are re-run in a further wave with 4x the space.
+//  - uastar_serve_*: a host thread admits requests by their estimated heap +
+//    partition bytes against a budget, gives each a resident slot whose search
+//    state (team state, heaps, partition) stays on the device between
+//    quanta, launches one persistent kernel per quantum that advances every
+//    resident request by a bounded number of rounds, retires finished ones
+//    and backfills from the queue.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <ctime>
+#include <numeric>
+#include <vector>
+
+#include "engine_internal.h"
+#include "ga_device.cuh"
+#include "ga_problems.cuh"
+#include "ga_search.cuh"
+
+using namespace uastar;
+
+namespace uastar {
+
+struct InstDesc {
+    int32_t kind, n, H, W, sx, sy, ex, ey;
+    uint64_t bm_word;     // first 32-bit word of the bitmap in the bitmap arena
+    uint64_t start_key;   // packed board (puzzle)
+    uint64_t tab_off;     // first slot of the dedup partition
+    uint32_t log2_slots;
+    uint32_t fresh;       // serving: state not yet initialised
+    uint64_t max_rounds;
+};
+
+struct InstOut {
+    uint32_t status, goal_slot;
+    unsigned long long goal_best, rounds, expanded, generated, pushed, inserted;
+};
+
+struct BatchArgs {
+    const InstDesc *descs;
+    uint32_t count;
+    uint32_t *queue;
+    const uint32_t *bitmaps;
+    const uint8_t *pdb3;
+    const uint8_t *pdb4;
+    Slot *tab;
+    uint8_t *heaps;        // per CTA: blockDim heaps x stride16 x 16 bytes
+    uint32_t stride16;     // heap stride in 16-byte entries (puzzles use 2x as 8-byte entries)
+    uint32_t *hsize;       // per CTA: blockDim
+    Cand *cand;            // per CTA: blockDim * 8
+    InstOut *outs;
+    TeamState *states;     // serving: per slot persisted team state
+    double max_load;
+    uint64_t budget;       // rounds per call (serving quantum) or ~0
+    int serving;           // 1: CTA b serves slot b; 0: work queue
+};
+
+__device__ void clear_partition(Slot *tab, uint64_t slots) {
+    uint4 *p = reinterpret_cast<uint4 *>(tab);
+    const uint4 v = make_uint4(~0u, ~0u, ~0u, ~0u);
+    for (uint64_t j = threadIdx.x; j < slots * 2; j += blockDim.x) p[j] = v;
+}
+
+__device__ void init_state(TeamState *st) {
+    memset(st, 0, sizeof(TeamState));
+    st->round_min[0] = st->round_min[1] = kInfCost;
+    st->goal_best = kInfCost;
+    st->goal_slot = kNone;
+    st->status = ST_RUNNING;
+}
+
+// Runs one instance on this CTA for up to `budget` rounds.
+__device__ uint32_t run_instance(const BatchArgs &a, const InstDesc &d, TeamState *st, uint8_t *heaps,
+                                 uint32_t *hs, Cand *cand, uint64_t budget) {
+    BlockTeam team{st};
+    Slot *tab = a.tab + d.tab_off;
+    const uint64_t slots = 1ull << d.log2_slots;
+    if (d.kind == UASTAR_KIND_GRID) {
+        GridProblem prob;
+        prob.bm = a.bitmaps + d.bm_word;
+        prob.H = d.H;
+        prob.W = d.W;
+        prob.sx = d.sx;
+        prob.sy = d.sy;
+        prob.ex = d.ex;
+        prob.ey = d.ey;
+        SearchMem<GridEntry> m{tab, slots - 1, (uint64_t)(slots * a.max_load), 4096u,
+                               reinterpret_cast<GridEntry *>(heaps), a.stride16, hs, cand, d.max_rounds};
+        return ga_search(prob, team, m, budget);
+    }
+    if (d.n == 4) {
+        PuzzleProblem<4> prob;
+        prob.pdb = a.pdb4;
+        prob.start = d.start_key;
+        prob.goal = PuzzleProblem<4>::goal_key();
+        SearchMem<PuzzleEntry> m{tab, slots - 1, (uint64_t)(slots * a.max_load), 4096u,
+                                 reinterpret_cast<PuzzleEntry *>(heaps), a.stride16 * 2, hs, cand,
+                                 d.max_rounds};
+        return ga_search(prob, team, m, budget);
+    }
+    PuzzleProblem<3> prob;
+    prob.pdb = a.pdb3;
+    prob.start = d.start_key;
+    prob.goal = PuzzleProblem<3>::goal_key();
+    SearchMem<PuzzleEntry> m{tab, slots - 1, (uint64_t)(slots * a.max_load), 4096u,
+                             reinterpret_cast<PuzzleEntry *>(heaps), a.stride16 * 2, hs, cand, d.max_rounds};
+    return ga_search(prob, team, m, budget);
+}
+
+__global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
+    __shared__ TeamState st;
+    __shared__ uint32_t s_next;
+    const uint32_t T = blockDim.x;
+    uint8_t *heaps = a.heaps + (size_t)blockIdx.x * T * a.stride16 * 16;
+    uint32_t *hs = a.hsize + (size_t)blockIdx.x * T;
+    Cand *cand = a.cand + (size_t)blockIdx.x * T * 8;
+    for (uint32_t iter = 0;; ++iter) {
+        if (a.serving) {
+            if (iter > 0 || blockIdx.x >= a.count) break;
+            if (threadIdx.x == 0) s_next = blockIdx.x;
+        } else if (threadIdx.x == 0) {
+            s_next = atomicAdd(a.queue, 1u);
+        }
+        __syncthreads();
+        const uint32_t i = s_next;
+        if (i >= a.count) break;
+        const InstDesc d = a.descs[i];
+        if (a.serving && d.kind == 0) break;  // empty serving slot
+        if (!a.serving || d.fresh) {
+            clear_partition(a.tab + d.tab_off, 1ull << d.log2_slots);
+            for (uint32_t j = threadIdx.x; j < T; j += T) hs[j] = 0;
+            if (threadIdx.x == 0) init_state(&st);
+        } else if (threadIdx.x == 0) {
+            st = a.states[i];
+        }
+        __syncthreads();
+        run_instance(a, d, &st, heaps, hs, cand, a.budget);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            InstOut o;
+            o.status = st.status;
+            o.goal_slot = st.goal_slot;
+            o.goal_best = st.goal_best;
+            o.rounds = st.round;
+            o.expanded = st.expanded;
+            o.generated = st.generated;
+            o.pushed = st.pushed;
+            o.inserted = st.inserted;
+            // a phase-2 error of the last round of a quantum is still in error2
+            if (o.status == ST_RUNNING && (st.error || st.error2[0] || st.error2[1]))
+                o.status = st.error ? st.error : (st.error2[0] ? st.error2[0] : st.error2[1]);
+            a.outs[i] = o;
+            if (a.serving) a.states[i] = st;
+        }
+        __syncthreads();
+    }
+}
+
+// One thread per finished instance walks its prev chain (goal -> start).
+__global__ void k_batch_walk(const InstDesc *descs, const InstOut *outs, const uint32_t *which,
+                             uint32_t nwhich, const Slot *tab, unsigned long long *keys,
+                             const uint64_t *key_off, const uint64_t *key_cap, unsigned long long *lens) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nwhich) return;
+    const uint32_t i = which[t];
+    const Slot *part = tab + descs[i].tab_off;
+    uint32_t s = outs[i].goal_slot;
+    const uint64_t cap = key_cap[t];
+    unsigned long long *out = keys + key_off[t];
+    uint64_t n = 0;
+    while (s != kNone && n < cap) {
+        out[n++] = __ldcg(&part[s].key);
+        s = __ldcg(&part[s].prev);
+    }
+    lens[t] = (s != kNone) ? cap + 1 : n;
+}
+
+}  // namespace uastar
+
+namespace {
+
+inline double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+inline uint64_t next_pow2_u64(uint64_t v) {
+    uint64_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+inline int log2_u64(uint64_t v) {
+    int l = 0;
+    while ((1ull << l) < v) ++l;
+    return l;
+}
+uint64_t pack_board(int n, const uint8_t *tiles) {
+    uint64_t k = 0;
+    for (int i = 0; i < n * n; ++i) k |= (uint64_t)(tiles[i] & 15) << (4 * i);
+    return k;
+}
+bool board_solvable(int n, const uint8_t *tiles) {
+    int inv = 0, brow = 0, seen = 0;
+    for (int i = 0; i < n * n; ++i) {
+        if (tiles[i] >= n * n || (seen >> tiles[i] & 1)) return false;
+        seen |= 1 << tiles[i];
+        if (!tiles[i]) {
+            brow = i / n;
+            continue;
+        }
+        for (int j = i + 1; j < n * n; ++j)
+            if (tiles[j] && tiles[j] < tiles[i]) ++inv;
+    }
+    if (n & 1) return (inv & 1) == 0;
+    return ((inv + brow) & 1) == ((n - 1) & 1);
+}
+
+// Estimated dedup nodes of an instance (a sizing hint; overflow is retried).
+uint64_t est_nodes(const uastar_instance &in) {
+    if (in.est_nodes > 0) return (uint64_t)in.est_nodes;
+    if (in.kind == UASTAR_KIND_GRID) return std::max<uint64_t>(4096, (uint64_t)in.H * in.W / 4);
+    // Puzzles start small; an instance that fills its partition is re-run
+    // in the next wave with 8x the space.
+    return in.n == 3 ? 32768 : 65536;
+}
+
+struct BatchPlan {
+    std::vector<InstDesc> descs;
+    std::vector<uint64_t> bm_words;  // packed bitmaps of all grid instances (32-bit words)
+    uint64_t total_slots = 0;
+};
+
+int32_t check_instance(const uastar_instance &in) {
+    if (in.kind == UASTAR_KIND_GRID) {
+        if (!in.words || in.H <= 0 || in.W <= 0 || (uint64_t)in.H * in.W >= (1ull << 32)) return UASTAR_BAD_INPUT;
+        if (in.sx < 0 || in.sx >= in.H || in.sy < 0 || in.sy >= in.W || in.ex < 0 || in.ex >= in.H ||
+            in.ey < 0 || in.ey >= in.W)
+            return UASTAR_BAD_INPUT;
+        return UASTAR_OK;
+    }
+    if (in.kind == UASTAR_KIND_PUZZLE && (in.n == 3 || in.n == 4)) {
+        int seen = 0;
+        for (int i = 0; i < in.n * in.n; ++i) {
+            if (in.tiles[i] >= in.n * in.n || (seen >> in.tiles[i] & 1)) return UASTAR_BAD_INPUT;
+            seen |= 1 << in.tiles[i];
+        }
+        return UASTAR_OK;
+    }
+    return UASTAR_BAD_INPUT;
+}
+
+struct BatchGeometry {
+    int T, ctas;
+    uint32_t stride16;
+    double load;
+};
+
+int32_t resolve_geometry(uastar_engine *eng, const uastar_batch_config *cfg, BatchGeometry *g) {
+    g->T = cfg && cfg->threads_per_instance > 0 ? cfg->threads_per_instance : 256;
+    g->T = std::max(32, std::min(512, (g->T + 31) / 32 * 32));
+    const uint32_t cap = cfg && cfg->heap_capacity > 0 ? (uint32_t)cfg->heap_capacity : 2048;
+    g->stride16 = (uint32_t)next_pow2_u64(cap + 1);
+    g->load = cfg && cfg->load_factor > 0 && cfg->load_factor < 1 ? cfg->load_factor : 0.5;
+    int occ = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch, g->T, 0);
+    if (e != cudaSuccess) return fail_cuda(eng, e, "occupancy");
+    occ = std::max(1, occ);
+    g->ctas = cfg && cfg->ctas > 0 ? cfg->ctas : eng->sms * occ;
+    return UASTAR_OK;
+}
+
+// Runs `idx` (indices into insts) as one wave; fills results for them.
+int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::vector<int> &idx,
+                 const BatchGeometry &g, const std::vector<int> &space_mult, bool use_graph,
+                 uastar_instance_result *results, uastar_batch_stats *stats, std::vector<int> *retry) {
+    cudaError_t e;
+    const int cnt = (int)idx.size();
+    // plan: order largest estimate first (longest-processing-time first)
+    std::vector<int> order(cnt);
+    std::iota(order.begin(), order.end(), 0);
+    std::vector<uint64_t> est(cnt);
+    for (int j = 0; j < cnt; ++j) est[j] = est_nodes(insts[idx[j]]) * (uint64_t)space_mult[j];
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return est[a] > est[b]; });
+
+    std::vector<InstDesc> descs(cnt);
+    std::vector<int> slot_of(cnt);  // position of wave instance j in descs
+    uint64_t bm_words = 0, tab_slots = 0;
+    for (int p = 0; p < cnt; ++p) {
+        const int j = order[p];
+        const uastar_instance &in = insts[idx[j]];
+        InstDesc d;
+        std::memset(&d, 0, sizeof d);
+        d.kind = in.kind;
+        d.n = in.n;
+        d.max_rounds = eng->cfg.max_rounds;
+        uint64_t slots = next_pow2_u64((uint64_t)((double)est[j] / g.load));
+        slots = std::max<uint64_t>(slots, 1u << 12);
+        d.log2_slots = (uint32_t)log2_u64(slots);
+        d.tab_off = tab_slots;
+        tab_slots += slots;
+        if (in.kind == UASTAR_KIND_GRID) {
+            d.H = in.H;
+            d.W = in.W;
+            d.sx = in.sx;
+            d.sy = in.sy;
+            d.ex = in.ex;
+            d.ey = in.ey;
+            d.bm_word = bm_words * 2;
+            bm_words += ((uint64_t)in.H * in.W + 63) / 64 + 2;
+        } else {
+            d.start_key = pack_board(in.n, in.tiles);
+        }
+        descs[p] = d;
+        slot_of[j] = p;
+    }
+    // device buffers
+    const size_t tab_b = tab_slots * sizeof(Slot);
+    const size_t heap_b = (size_t)g.ctas * g.T * g.stride16 * 16;
+    if ((e = eng->b_tab.ensure(tab_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc partitions");
+    if ((e = eng->b_heaps.ensure(heap_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc heap slices");
+    if ((e = eng->b_hsize.ensure((size_t)g.ctas * g.T * 4)) != cudaSuccess) return fail_cuda(eng, e, "alloc");
+    if ((e = eng->b_cand.ensure((size_t)g.ctas * g.T * 8 * sizeof(Cand))) != cudaSuccess)
+        return fail_cuda(eng, e, "alloc");
+    if ((e = eng->b_desc.ensure(cnt * sizeof(InstDesc))) != cudaSuccess) return fail_cuda(eng, e, "alloc");
+    if ((e = eng->b_out.ensure(cnt * sizeof(InstOut))) != cudaSuccess) return fail_cuda(eng, e, "alloc");
+    if ((e = eng->b_queue.ensure(64)) != cudaSuccess) return fail_cuda(eng, e, "alloc");
+    if ((e = eng->b_bitmaps.ensure(std::max<size_t>(16, bm_words * 8))) != cudaSuccess)
+        return fail_cuda(eng, e, "alloc bitmaps");
+    // bitmaps H2D (one copy per grid)
+    for (int p = 0; p < cnt; ++p) {
+        const int j = order[p];
+        const uastar_instance &in = insts[idx[j]];
+        if (in.kind != UASTAR_KIND_GRID) continue;
+        const size_t nb = (((uint64_t)in.H * in.W + 63) / 64) * 8;
+        e = cudaMemcpyAsync(eng->b_bitmaps.as<uint32_t>() + descs[p].bm_word, in.words, nb,
+                            cudaMemcpyHostToDevice, eng->stream);
+        if (e != cudaSuccess) return fail_cuda(eng, e, "bitmap upload");
+    }
+    if ((e = cudaMemcpyAsync(eng->b_desc.p, descs.data(), cnt * sizeof(InstDesc), cudaMemcpyHostToDevice,
+                             eng->stream)) != cudaSuccess)
+        return fail_cuda(eng, e, "desc upload");
+
+    BatchArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.descs = eng->b_desc.as<InstDesc>();
+    a.count = (uint32_t)cnt;
+    a.queue = eng->b_queue.as<uint32_t>();
+    a.bitmaps = eng->b_bitmaps.as<uint32_t>();
+    a.pdb3 = eng->pdb[3].as<uint8_t>();
+    a.pdb4 = eng->pdb[4].as<uint8_t>();
+    a.tab = eng->b_tab.as<Slot>();
+    a.heaps = eng->b_heaps.as<uint8_t>();
+    a.stride16 = g.stride16;
+    a.hsize = eng->b_hsize.as<uint32_t>();
+    a.cand = eng->b_cand.as<Cand>();
+    a.outs = eng->b_out.as<InstOut>();
+    a.max_load = 0.9;
+    a.budget = ~0ull;
+    a.serving = 0;
+    const int ctas = std::min(g.ctas, cnt);
+
+    cudaEvent_t k0, k1;
+    cudaEventCreate(&k0);
+    cudaEventCreate(&k1);
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    auto enqueue = [&]() {
+        cudaMemsetAsync(eng->b_queue.p, 0, 4, eng->stream);
+        k_batch<<<ctas, g.T, 0, eng->stream>>>(a);
+    };
+    cudaEventRecord(k0, eng->stream);
+    if (use_graph) {
+        e = cudaStreamBeginCapture(eng->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            enqueue();
+            e = cudaStreamEndCapture(eng->stream, &graph);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+        if (e == cudaSuccess) e = cudaGraphLaunch(exec, eng->stream);
+    } else {
+        enqueue();
+        e = cudaGetLastError();
+    }
+    eng->launches++;
+    cudaEventRecord(k1, eng->stream);
+    if (e != cudaSuccess) {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        return fail_cuda(eng, e, "batch launch");
+    }
+    std::vector<InstOut> outs(cnt);
+    e = cudaMemcpyAsync(outs.data(), eng->b_out.p, cnt * sizeof(InstOut), cudaMemcpyDeviceToHost, eng->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(eng->stream);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail_cuda(eng, e, "batch kernel");
+    float kms = 0;
+    cudaEventElapsedTime(&kms, k0, k1);
+    cudaEventDestroy(k0);
+    cudaEventDestroy(k1);
+    if (stats) stats->kernel_ms += kms;
+
+    // paths of solved instances: one walker thread each
+    std::vector<uint32_t> which;
+    std::vector<uint64_t> koff, kcap;
+    uint64_t ktot = 0;
+    for (int p = 0; p < cnt; ++p) {
+        if (outs[p].status != ST_OK) continue;
+        const uastar_instance &in = insts[idx[order[p]]];
+        const uint64_t cap = in.kind == UASTAR_KIND_GRID ? 8ull * (in.H + in.W) + 64 : 512;
+        which.push_back((uint32_t)p);
+        koff.push_back(ktot);
+        kcap.push_back(cap);
+        ktot += cap;
+    }
+    std::vector<unsigned long long> keys(ktot), lens(which.size());
+    if (!which.empty()) {
+        const size_t nw = which.size();
+        const size_t need = ktot * 8 + nw * (4 + 8 + 8 + 8) + 256;
+        if ((e = eng->b_walk.ensure(need)) != cudaSuccess) return fail_cuda(eng, e, "alloc walk");
+        char *base = eng->b_walk.as<char>();
+        unsigned long long *d_keys = reinterpret_cast<unsigned long long *>(base);
+        uint64_t *d_off = reinterpret_cast<uint64_t *>(base + ktot * 8);
+        uint64_t *d_cap = d_off + nw;
+        unsigned long long *d_len = reinterpret_cast<unsigned long long *>(d_cap + nw);
+        uint32_t *d_which = reinterpret_cast<uint32_t *>(d_len + nw);
+        cudaMemcpyAsync(d_off, koff.data(), nw * 8, cudaMemcpyHostToDevice, eng->stream);
+        cudaMemcpyAsync(d_cap, kcap.data(), nw * 8, cudaMemcpyHostToDevice, eng->stream);
+        cudaMemcpyAsync(d_which, which.data(), nw * 4, cudaMemcpyHostToDevice, eng->stream);
+        k_batch_walk<<<(unsigned)((nw + 127) / 128), 128, 0, eng->stream>>>(
+            eng->b_desc.as<InstDesc>(), eng->b_out.as<InstOut>(), d_which, (uint32_t)nw, eng->b_tab.as<Slot>(),
+            d_keys, d_off, d_cap, d_len);
+        eng->launches++;
+        cudaMemcpyAsync(lens.data(), d_len, nw * 8, cudaMemcpyDeviceToHost, eng->stream);
+        cudaMemcpyAsync(keys.data(), d_keys, ktot * 8, cudaMemcpyDeviceToHost, eng->stream);
+        if ((e = cudaStreamSynchronize(eng->stream)) != cudaSuccess) return fail_cuda(eng, e, "batch walk");
+    }
+    std::vector<int> walk_of(cnt, -1);
+    for (size_t w = 0; w < which.size(); ++w) walk_of[which[w]] = (int)w;
+
+    for (int j = 0; j < cnt; ++j) {
+        const int p = slot_of[j];
+        const InstOut &o = outs[p];
+        const uastar_instance &in = insts[idx[j]];
+        uastar_instance_result &r = results[idx[j]];
+        r.attempts += 1;
+        r.status = (int32_t)o.status;
+        r.expanded += (int64_t)o.expanded;
+        r.generated += (int64_t)o.generated;
+        r.rounds += (int64_t)o.rounds;
+        if (stats) {
+            stats->expanded += (int64_t)o.expanded;
+            stats->generated += (int64_t)o.generated;
+        }
+        if ((o.status == ST_HASH_FULL || o.status == ST_HEAP_OVERFLOW) && retry) {
+            retry->push_back(idx[j]);
+            continue;
+        }
+        if (o.status != ST_OK) continue;
+        const int w = walk_of[p];
+        const uint64_t len = lens[w];
+        if (len > kcap[w]) {
+            r.status = UASTAR_ARENA_FULL;
+            continue;
+        }
+        // keys are goal -> start
+        const unsigned long long *kk = keys.data() + koff[w];
+        if (in.kind == UASTAR_KIND_GRID) {
+            r.straight = (int64_t)(o.goal_best >> 32);
+            r.diagonal = (int64_t)(o.goal_best & 0xffffffffu);
+            std::vector<int32_t> path(len);
+            for (uint64_t t = 0; t < len; ++t) path[t] = (int32_t)kk[len - 1 - t];
+            int64_t a2 = 0, b2 = 0;
+            float fc = 0;
+            if (uastar_validate_grid_path(in.words, in.H, in.W, in.sx, in.sy, in.ex, in.ey, path.data(),
+                                          (int64_t)len, &a2, &b2, &fc) != UASTAR_OK ||
+                a2 != r.straight || b2 != r.diagonal) {
+                r.status = UASTAR_CUDA_ERROR;
+                eng->set_err("batched engine returned a path that fails host validation");
+                continue;
+            }
+            r.cost = fc;
+        } else {
+            r.steps = (int32_t)o.goal_best;
+            std::vector<int32_t> moves;
+            auto blank = [&](uint64_t k) {
+                for (int c = 0; c < in.n * in.n; ++c)
+                    if (((k >> (4 * c)) & 15) == 0) return c;
+                return -1;
+            };
+            for (uint64_t t = len - 1; t >= 1; --t) {
+                const int pb = blank(kk[t]), cb = blank(kk[t - 1]);
+                moves.push_back(cb - pb == in.n ? 0 : cb - pb == -in.n ? 1 : cb - pb == 1 ? 2 : 3);
+            }
+            if ((int64_t)moves.size() != r.steps ||
+                uastar_validate_puzzle_moves(in.n, in.tiles, moves.data(), (int64_t)moves.size()) != UASTAR_OK) {
+                r.status = UASTAR_CUDA_ERROR;
+                eng->set_err("batched engine returned moves that fail host validation");
+                continue;
+            }
+        }
+    }
+    if (stats) {
+        stats->waves += 1;
+        stats->partition_bytes = std::max<int64_t>(stats->partition_bytes, (int64_t)tab_b);
+    }
+    return UASTAR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int32_t count,
+                           const uastar_batch_config *cfg, uastar_instance_result *results,
+                           uastar_batch_stats *stats) {
+    if (!eng || !insts || count < 0 || !results) return UASTAR_BAD_INPUT;
+    cudaSetDevice(eng->device);
+    const double t0 = now_ms();
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    std::memset(results, 0, sizeof(uastar_instance_result) * (size_t)count);
+    BatchGeometry g;
+    int32_t rc = resolve_geometry(eng, cfg, &g);
+    if (rc) return rc;
+    std::vector<int> todo;
+    for (int i = 0; i < count; ++i) {
+        const uastar_instance &in = insts[i];
+        if (check_instance(in) != UASTAR_OK) {
+            results[i].status = UASTAR_BAD_INPUT;
+            continue;
+        }
+        if (in.kind == UASTAR_KIND_PUZZLE) {
+            if (!eng->pdb_ready[in.n]) {
+                results[i].status = UASTAR_BAD_INPUT;
+                eng->set_err("pattern database not resident for a puzzle instance");
+                continue;
+            }
+            if (!board_solvable(in.n, in.tiles)) {
+                results[i].status = UASTAR_NO_SOLUTION;
+                continue;
+            }
+        }
+        todo.push_back(i);
+    }
+    std::vector<int> mult(count, 1);
+    BatchGeometry gw = g;
+    const bool use_graph = !cfg || cfg->use_graph != 0 || cfg->threads_per_instance == 0;
+    for (int wave = 0; wave < 5 && !todo.empty(); ++wave) {
+        std::vector<int> retry, m(todo.size());
+        for (size_t j = 0; j < todo.size(); ++j) m[j] = mult[todo[j]];
+        rc = run_wave(eng, insts, todo, gw, m, use_graph, results, stats, &retry);
+        if (rc) return rc;
+        for (int i : retry) mult[i] *= 8;
+        bool heap_over = false;
+        for (int i : retry) heap_over |= results[i].status == UASTAR_HEAP_OVERFLOW;
+        if (heap_over) gw.stride16 *= 4;
+        // a retry wave runs fewer instances: fewer CTAs keep the heap slices small
+        gw.ctas = std::min<int>(g.ctas, std::max<int>(1, (int)retry.size()));
+        todo.swap(retry);
+    }
+    if (stats) {
+        stats->wall_ms = now_ms() - t0;
+        stats->ctas = g.ctas;
+        stats->threads_per_instance = g.T;
+        stats->heap_capacity = (int32_t)g.stride16 - 1;
+        stats->load_factor = g.load;
+    }
+    for (int i = 0; i < count; ++i) results[i].latency_ms = now_ms() - t0;
+    return UASTAR_OK;
+}
+
+int32_t uastar_autotune(uastar_engine *eng, const uastar_instance *sample, int32_t count,
+                        uastar_batch_config *best) {
+    if (!eng || !sample || count <= 0 || !best) return UASTAR_BAD_INPUT;
+    const int Ts[] = {128, 256, 512};
+    const int caps[] = {1024, 4096};
+    const double loads[] = {0.35, 0.6};
+    std::vector<uastar_instance_result> res(count);
+    double best_ms = 1e300;
+    uastar_batch_config pick{};
+    for (int T : Ts)
+        for (int cap : caps)
+            for (double ld : loads) {
+                uastar_batch_config c{};
+                c.threads_per_instance = T;
+                c.heap_capacity = cap;
+                c.load_factor = ld;
+                c.use_graph = 1;
+                uastar_batch_stats s;
+                if (uastar_batch_solve(eng, sample, count, &c, res.data(), &s) != UASTAR_OK) continue;
+                bool ok = true;
+                for (auto &r : res) ok &= (r.status == UASTAR_OK || r.status == UASTAR_NO_SOLUTION);
+                if (!ok) continue;
+                if (s.wall_ms < best_ms) {
+                    best_ms = s.wall_ms;
+                    pick = c;
+                }
+            }
+    if (best_ms >= 1e300) {
+        eng->set_err("autotune: no configuration solved the sample");
+        return UASTAR_CUDA_ERROR;
+    }
+    *best = pick;
+    return UASTAR_OK;
+}
+
+}  // extern "C"
+
+// ===================================================================== serving
+namespace uastar {
+
+// First-fit allocator over [0, capacity) units, for the dedup-partition and
+// bitmap arenas of the serving loop.  Host-side bookkeeping only.
+class RangeAlloc {
+public:
+    void reset(uint64_t capacity) {
+        free_.clear();
+        if (capacity) free_[0] = capacity;
+        cap_ = capacity;
+        used_ = 0;
+    }
+    bool alloc(uint64_t n, uint64_t align, uint64_t *off) {
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            const uint64_t start = (it->first + align - 1) / align * align;
+            const uint64_t end = it->first + it->second;
+            if (start + n > end) continue;
+            const uint64_t s0 = it->first;
+            free_.erase(it);
+            if (start > s0) free_[s0] = start - s0;
+            if (end > start + n) free_[start + n] = end - (start + n);
+            *off = start;
+            used_ += n;
+            return true;
+        }
+        return false;
+    }
+    void release(uint64_t off, uint64_t n) {
+        used_ -= n;
+        auto it = free_.emplace(off, n).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    uint64_t used() const { return used_; }
+    uint64_t capacity() const { return cap_; }
+
+private:
+    std::map<uint64_t, uint64_t> free_;
+    uint64_t cap_ = 0, used_ = 0;
+};
+
+struct ServeReq {
+    int64_t id = 0;
+    uastar_instance inst{};
+    std::vector<uint64_t> words;  // owned copy of the grid bitmap
+    double arrival_s = 0;
+    uint64_t mult = 1;
+    int attempts = 0;
+    uastar_instance_result acc{};
+};
+
+struct ServeSlotState {
+    bool busy = false;
+    ServeReq req;
+    uint64_t tab_off = 0, tab_n = 0, bm_off = 0, bm_n = 0;
+};
+
+struct ServeState {
+    uastar_engine *eng = nullptr;
+    uastar_serve_config cfg{};
+    int T = 256, S = 0;
+    uint32_t stride16 = 2048;
+    uint64_t heap_bytes = 0;
+    std::thread th;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<ServeReq> incoming;
+    std::vector<int64_t> cancels;
+    std::deque<uastar_serve_completion> done;
+    bool draining = false, abort_now = false;
+    int64_t next_id = 0;
+    int64_t outstanding = 0;  // submitted and not yet completed
+    uastar_serve_stats stats{};
+    int32_t loop_error = UASTAR_OK;
+    // device state
+    DevBuf tab, bitmaps, heaps, hsize, cand, descs, outs, states, walk;
+    RangeAlloc tab_alloc, bm_alloc;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t q0 = nullptr, q1 = nullptr;
+};
+
+static void serve_complete(ServeState *S, ServeReq &r, int32_t status) {
+    uastar_serve_completion c;
+    c.id = r.id;
+    c.result = r.acc;
+    c.result.status = status;
+    c.result.attempts = r.attempts;
+    c.result.latency_ms = (uastar_now_s() - r.arrival_s) * 1e3;
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->done.push_back(c);
+    S->outstanding -= 1;
+    S->stats.completed += 1;
+    if (status == UASTAR_CANCELLED) S->stats.cancelled += 1;
+    if (status == UASTAR_REJECTED) S->stats.rejected += 1;
+}
+
+static uint64_t serve_partition_slots(const ServeState *S, const ServeReq &r) {
+    const double load = S->cfg.load_factor > 0 && S->cfg.load_factor < 1 ? S->cfg.load_factor : 0.5;
+    uint64_t slots = next_pow2_u64((uint64_t)((double)est_nodes(r.inst) * (double)r.mult / load));
+    return std::max<uint64_t>(slots, 1u << 12);
+}
+
+static void serve_loop(ServeState *S) {
+    uastar_engine *eng = S->eng;
+    cudaSetDevice(eng->device);
+    std::vector<ServeSlotState> slots(S->S);
+    std::vector<ServeReq> pending;  // kept sorted by arrival
+    std::vector<InstDesc> descs(S->S);
+    std::vector<InstOut> outs(S->S);
+    std::memset(descs.data(), 0, descs.size() * sizeof(InstDesc));
+    cudaError_t e;
+    auto fail = [&](cudaError_t err, const char *what) {
+        fail_cuda(eng, err, what);
+        S->loop_error = UASTAR_CUDA_ERROR;
+    };
+    for (;;) {
+        // 1. intake
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            while (!S->incoming.empty()) {
+                pending.push_back(std::move(S->incoming.front()));
+                S->incoming.pop_front();
+            }
+            std::vector<int64_t> cancels;
+            cancels.swap(S->cancels);
+            lk.unlock();
+            std::stable_sort(pending.begin(), pending.end(),
+                             [](const ServeReq &a, const ServeReq &b) { return a.arrival_s < b.arrival_s; });
+            for (int64_t cid : cancels) {
+                for (size_t i = 0; i < pending.size(); ++i)
+                    if (pending[i].id == cid) {
+                        serve_complete(S, pending[i], UASTAR_CANCELLED);
+                        pending.erase(pending.begin() + i);
+                        break;
+                    }
+                for (int s = 0; s < S->S; ++s)
+                    if (slots[s].busy && slots[s].req.id == cid) {
+                        serve_complete(S, slots[s].req, UASTAR_CANCELLED);
+                        S->tab_alloc.release(slots[s].tab_off, slots[s].tab_n);
+                        if (slots[s].bm_n) S->bm_alloc.release(slots[s].bm_off, slots[s].bm_n);
+                        slots[s] = ServeSlotState();
+                        descs[s].kind = 0;
+                    }
+            }
+        }
+        if (S->loop_error) break;
+        // 2. admission: arrived requests, in arrival order, while a slot and budget are free
+        const double now = uastar_now_s();
+        size_t taken = 0;
+        int free_slot = 0;
+        for (; taken < pending.size(); ++taken) {
+            ServeReq &r = pending[taken];
+            if (r.arrival_s > now) break;
+            while (free_slot < S->S && slots[free_slot].busy) ++free_slot;
+            if (free_slot >= S->S) break;
+            const uint64_t tn = serve_partition_slots(S, r);
+            const uint64_t bn = r.inst.kind == UASTAR_KIND_GRID ? r.words.size() + 2 : 0;
+            if (tn > S->tab_alloc.capacity() || bn > S->bm_alloc.capacity()) {
+                serve_complete(S, r, UASTAR_REJECTED);  // can never fit the budget
+                continue;
+            }
+            uint64_t toff = 0, boff = 0;
+            if (!S->tab_alloc.alloc(tn, 1, &toff)) break;  // wait for memory to free up
+            if (bn && !S->bm_alloc.alloc(bn, 2, &boff)) {
+                S->tab_alloc.release(toff, tn);
+                break;
+            }
+            ServeSlotState &sl = slots[free_slot];
+            sl.busy = true;
+            sl.tab_off = toff;
+            sl.tab_n = tn;
+            sl.bm_off = boff;
+            sl.bm_n = bn;
+            sl.req = std::move(r);
+            sl.req.attempts += 1;
+            InstDesc d;
+            std::memset(&d, 0, sizeof d);
+            d.kind = sl.req.inst.kind;
+            d.n = sl.req.inst.n;
+            d.max_rounds = eng->cfg.max_rounds;
+            d.tab_off = toff;
+            d.log2_slots = (uint32_t)log2_u64(tn);
+            d.fresh = 1;
+            if (d.kind == UASTAR_KIND_GRID) {
+                d.H = sl.req.inst.H;
+                d.W = sl.req.inst.W;
+                d.sx = sl.req.inst.sx;
+                d.sy = sl.req.inst.sy;
+                d.ex = sl.req.inst.ex;
+                d.ey = sl.req.inst.ey;
+                d.bm_word = boff * 2;
+                e = cudaMemcpyAsync(S->bitmaps.as<uint64_t>() + boff, sl.req.words.data(),
+                                    sl.req.words.size() * 8, cudaMemcpyHostToDevice, S->stream);
+                if (e != cudaSuccess) fail(e, "serve bitmap upload");
+            } else {
+                d.start_key = pack_board(d.n, sl.req.inst.tiles);
+            }
+            descs[free_slot] = d;
+        }
+        pending.erase(pending.begin(), pending.begin() + taken);
+        int resident = 0;
+        for (auto &sl : slots) resident += sl.busy;
+        S->stats.peak_resident = std::max(S->stats.peak_resident, resident);
+        S->stats.peak_budget_gb =
+            std::max(S->stats.peak_budget_gb, ((double)S->tab_alloc.used() * sizeof(Slot) +
+                                               (double)S->bm_alloc.used() * 8 + (double)S->heap_bytes) /
+                                                  1e9);
+        if (resident == 0) {
+            std::unique_lock<std::mutex> lk(S->mu);
+            if (S->abort_now || (S->draining && S->outstanding == 0)) break;
+            double wait_s = 0.002;
+            if (!pending.empty()) wait_s = std::max(0.0, std::min(wait_s, pending.front().arrival_s - now));
+            if (S->incoming.empty() && S->cancels.empty())
+                S->cv.wait_for(lk, std::chrono::duration<double>(wait_s));
+            continue;
+        }
+        // 3. one quantum over all resident requests
+        if ((e = cudaMemcpyAsync(S->descs.p, descs.data(), S->S * sizeof(InstDesc), cudaMemcpyHostToDevice,
+                                 S->stream)) != cudaSuccess) {
+            fail(e, "serve desc upload");
+            break;
+        }
+        BatchArgs a;
+        std::memset(&a, 0, sizeof a);
+        a.descs = S->descs.as<InstDesc>();
+        a.count = (uint32_t)S->S;
+        a.bitmaps = S->bitmaps.as<uint32_t>();
+        a.pdb3 = eng->pdb[3].as<uint8_t>();
+        a.pdb4 = eng->pdb[4].as<uint8_t>();
+        a.tab = S->tab.as<Slot>();
+        a.heaps = S->heaps.as<uint8_t>();
+        a.stride16 = S->stride16;
+        a.hsize = S->hsize.as<uint32_t>();
+        a.cand = S->cand.as<Cand>();
+        a.outs = S->outs.as<InstOut>();
+        a.states = S->states.as<TeamState>();
+        a.max_load = 0.9;
+        a.budget = (uint64_t)(S->cfg.rounds_per_quantum > 0 ? S->cfg.rounds_per_quantum : 256);
+        a.serving = 1;
+        cudaEventRecord(S->q0, S->stream);
+        k_batch<<<S->S, S->T, 0, S->stream>>>(a);
+        eng->launches++;
+        cudaEventRecord(S->q1, S->stream);
+        e = cudaGetLastError();
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(outs.data(), S->outs.p, S->S * sizeof(InstOut), cudaMemcpyDeviceToHost, S->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(S->stream);
+        if (e != cudaSuccess) {
+            fail(e, "serve quantum");
+            break;
+        }
+        float qms = 0;
+        cudaEventElapsedTime(&qms, S->q0, S->q1);
+        S->stats.quanta += 1;
+        S->stats.busy_ms += qms;
+        // 4. retire finished requests
+        std::vector<uint32_t> which;
+        std::vector<uint64_t> koff, kcap;
+        uint64_t ktot = 0;
+        for (int s = 0; s < S->S; ++s) {
+            if (!slots[s].busy) continue;
+            descs[s].fresh = 0;
+            if (outs[s].status == ST_RUNNING) continue;
+            if (outs[s].status == ST_OK) {
+                const auto &in = slots[s].req.inst;
+                const uint64_t cap = in.kind == UASTAR_KIND_GRID ? 8ull * (in.H + in.W) + 64 : 512;
+                which.push_back((uint32_t)s);
+                koff.push_back(ktot);
+                kcap.push_back(cap);
+                ktot += cap;
+            }
+        }
+        std::vector<unsigned long long> keys(ktot), lens(which.size());
+        if (!which.empty()) {
+            const size_t nw = which.size();
+            if ((e = S->walk.ensure(ktot * 8 + nw * 32 + 256)) != cudaSuccess) {
+                fail(e, "serve walk alloc");
+                break;
+            }
+            char *base = S->walk.as<char>();
+            unsigned long long *d_keys = reinterpret_cast<unsigned long long *>(base);
+            uint64_t *d_off = reinterpret_cast<uint64_t *>(base + ktot * 8);
+            uint64_t *d_cap = d_off + nw;
+            unsigned long long *d_len = reinterpret_cast<unsigned long long *>(d_cap + nw);
+            uint32_t *d_which = reinterpret_cast<uint32_t *>(d_len + nw);
+            cudaMemcpyAsync(d_off, koff.data(), nw * 8, cudaMemcpyHostToDevice, S->stream);
+            cudaMemcpyAsync(d_cap, kcap.data(), nw * 8, cudaMemcpyHostToDevice, S->stream);
+            cudaMemcpyAsync(d_which, which.data(), nw * 4, cudaMemcpyHostToDevice, S->stream);
+            k_batch_walk<<<(unsigned)((nw + 127) / 128), 128, 0, S->stream>>>(
+                S->descs.as<InstDesc>(), S->outs.as<InstOut>(), d_which, (uint32_t)nw, S->tab.as<Slot>(), d_keys,
+                d_off, d_cap, d_len);
+            eng->launches++;
+            cudaMemcpyAsync(lens.data(), d_len, nw * 8, cudaMemcpyDeviceToHost, S->stream);
+            cudaMemcpyAsync(keys.data(), d_keys, ktot * 8, cudaMemcpyDeviceToHost, S->stream);
+            if ((e = cudaStreamSynchronize(S->stream)) != cudaSuccess) {
+                fail(e, "serve walk");
+                break;
+            }
+        }
+        std::vector<int> walk_of(S->S, -1);
+        for (size_t w = 0; w < which.size(); ++w) walk_of[which[w]] = (int)w;
+        for (int s = 0; s < S->S; ++s) {
+            ServeSlotState &sl = slots[s];
+            if (!sl.busy || outs[s].status == ST_RUNNING) continue;
+            const InstOut &o = outs[s];
+            ServeReq &r = sl.req;
+            r.acc.expanded += (int64_t)o.expanded;
+            r.acc.generated += (int64_t)o.generated;
+            r.acc.rounds += (int64_t)o.rounds;
+            int32_t status = (int32_t)o.status;
+            S->tab_alloc.release(sl.tab_off, sl.tab_n);
+            if (sl.bm_n) S->bm_alloc.release(sl.bm_off, sl.bm_n);
+            descs[s].kind = 0;
+            if ((status == ST_HASH_FULL || status == ST_HEAP_OVERFLOW) && r.attempts < 5) {
+                r.mult *= 8;  // re-queue with a larger partition, ahead of later arrivals
+                pending.insert(pending.begin(), std::move(r));
+                sl = ServeSlotState();
+                continue;
+            }
+            if (status == ST_OK) {
+                const int w = walk_of[s];
+                const uint64_t len = lens[w];
+                const unsigned long long *kk = keys.data() + koff[w];
+                const auto &in = r.inst;
+                if (len > kcap[w]) {
+                    status = UASTAR_ARENA_FULL;
+                } else if (in.kind == UASTAR_KIND_GRID) {
+                    r.acc.straight = (int64_t)(o.goal_best >> 32);
+                    r.acc.diagonal = (int64_t)(o.goal_best & 0xffffffffu);
+                    std::vector<int32_t> path(len);
+                    for (uint64_t t = 0; t < len; ++t) path[t] = (int32_t)kk[len - 1 - t];
+                    int64_t a2 = 0, b2 = 0;
+                    float fc = 0;
+                    if (uastar_validate_grid_path(r.words.data(), in.H, in.W, in.sx, in.sy, in.ex, in.ey,
+                                                  path.data(), (int64_t)len, &a2, &b2, &fc) != UASTAR_OK ||
+                        a2 != r.acc.straight || b2 != r.acc.diagonal)
+                        status = UASTAR_CUDA_ERROR;
+                    r.acc.cost = fc;
+                } else {
+                    r.acc.steps = (int32_t)o.goal_best;
+                    std::vector<int32_t> moves;
+                    auto blank = [&](uint64_t k) {
+                        for (int c = 0; c < in.n * in.n; ++c)
+                            if (((k >> (4 * c)) & 15) == 0) return c;
+                        return -1;
+                    };
+                    for (uint64_t t = len - 1; t >= 1; --t) {
+                        const int pb = blank(kk[t]), cb = blank(kk[t - 1]);
+                        moves.push_back(cb - pb == in.n ? 0 : cb - pb == -in.n ? 1 : cb - pb == 1 ? 2 : 3);
+                    }
+                    if ((int64_t)moves.size() != r.acc.steps ||
+                        uastar_validate_puzzle_moves(in.n, in.tiles, moves.data(), (int64_t)moves.size()) !=
+                            UASTAR_OK)
+                        status = UASTAR_CUDA_ERROR;
+                }
+            }
+            serve_complete(S, r, status);
+            sl = ServeSlotState();
+        }
+    }
+    // drain: anything left is reported as cancelled
+    for (auto &r : pending) serve_complete(S, r, UASTAR_CANCELLED);
+    for (auto &sl : slots)
+        if (sl.busy) serve_complete(S, sl.req, UASTAR_CANCELLED);
+    std::deque<ServeReq> rest;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        rest.swap(S->incoming);
+    }
+    for (auto &r : rest) serve_complete(S, r, UASTAR_CANCELLED);
+}
+
+}  // namespace uastar
+
+extern "C" {
+
+double uastar_now_s(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+int32_t uastar_serve_start(uastar_engine *eng, const uastar_serve_config *cfg) {
+    if (!eng) return UASTAR_BAD_INPUT;
+    if (eng->serve) {
+        eng->set_err("serving loop already running");
+        return UASTAR_BAD_INPUT;
+    }
+    cudaSetDevice(eng->device);
+    auto *S = new ServeState();
+    S->eng = eng;
+    if (cfg) S->cfg = *cfg;
+    if (!(S->cfg.hbm_budget_gb > 0)) S->cfg.hbm_budget_gb = 120.0;
+    S->T = S->cfg.threads_per_instance > 0 ? std::max(32, std::min(512, (S->cfg.threads_per_instance + 31) / 32 * 32))
+                                           : 256;
+    S->stride16 = (uint32_t)next_pow2_u64((uint64_t)(S->cfg.heap_capacity > 0 ? S->cfg.heap_capacity : 2048) + 1);
+    int occ = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch, S->T, 0);
+    if (e != cudaSuccess) {
+        delete S;
+        return fail_cuda(eng, e, "occupancy");
+    }
+    const int max_slots = eng->sms * std::max(1, occ);
+    S->S = S->cfg.slots > 0 ? std::min(S->cfg.slots, max_slots) : max_slots;
+    const double budget_b = S->cfg.hbm_budget_gb * 1e9;
+    S->heap_bytes = (uint64_t)S->S * S->T * S->stride16 * 16;
+    const uint64_t bm_words = (uint64_t)(budget_b * 0.05 / 8);
+    const double tab_b = budget_b - (double)S->heap_bytes - (double)bm_words * 8;
+    if (tab_b < (double)(1u << 20) * sizeof(Slot)) {
+        delete S;
+        eng->set_err("serving budget too small for the heap slices");
+        return UASTAR_BAD_INPUT;
+    }
+    const uint64_t tab_slots = (uint64_t)(tab_b / sizeof(Slot));
+    S->tab_alloc.reset(tab_slots);
+    S->bm_alloc.reset(bm_words);
+    if ((e = S->tab.ensure(tab_slots * sizeof(Slot))) != cudaSuccess ||
+        (e = S->bitmaps.ensure(bm_words * 8 + 64)) != cudaSuccess ||
+        (e = S->heaps.ensure(S->heap_bytes)) != cudaSuccess ||
+        (e = S->hsize.ensure((size_t)S->S * S->T * 4)) != cudaSuccess ||
+        (e = S->cand.ensure((size_t)S->S * S->T * 8 * sizeof(Cand))) != cudaSuccess ||
+        (e = S->descs.ensure((size_t)S->S * sizeof(InstDesc))) != cudaSuccess ||
+        (e = S->outs.ensure((size_t)S->S * sizeof(InstOut))) != cudaSuccess ||
+        (e = S->states.ensure((size_t)S->S * sizeof(TeamState))) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreate(&S->q0)) != cudaSuccess || (e = cudaEventCreate(&S->q1)) != cudaSuccess) {
+        for (DevBuf *b : {&S->tab, &S->bitmaps, &S->heaps, &S->hsize, &S->cand, &S->descs, &S->outs, &S->states})
+            b->release();
+        delete S;
+        return fail_cuda(eng, e, "serving allocation");
+    }
+    eng->serve = S;
+    S->th = std::thread(serve_loop, S);
+    return UASTAR_OK;
+}
+
+int64_t uastar_serve_submit(uastar_engine *eng, const uastar_instance *inst, double arrival_s) {
+    if (!eng || !eng->serve || !inst) return -UASTAR_BAD_INPUT;
+    ServeState *S = eng->serve;
+    if (check_instance(*inst) != UASTAR_OK) return -UASTAR_BAD_INPUT;
+    if (inst->kind == UASTAR_KIND_PUZZLE && !eng->pdb_ready[inst->n]) return -UASTAR_BAD_INPUT;
+    ServeReq r;
+    r.inst = *inst;
+    r.arrival_s = arrival_s > 0 ? arrival_s : uastar_now_s();
+    if (inst->kind == UASTAR_KIND_GRID) {
+        const size_t nw = ((uint64_t)inst->H * inst->W + 63) / 64;
+        r.words.assign(inst->words, inst->words + nw);
+        r.inst.words = nullptr;
+    }
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (S->draining) return -UASTAR_BAD_INPUT;
+    r.id = S->next_id++;
+    S->stats.submitted += 1;
+    S->outstanding += 1;
+    const int64_t id = r.id;
+    if (inst->kind == UASTAR_KIND_PUZZLE && !board_solvable(inst->n, inst->tiles)) {
+        uastar_serve_completion c;
+        std::memset(&c, 0, sizeof c);
+        c.id = id;
+        c.result.status = UASTAR_NO_SOLUTION;
+        S->done.push_back(c);
+        S->outstanding -= 1;
+        S->stats.completed += 1;
+        return id;
+    }
+    S->incoming.push_back(std::move(r));
+    S->cv.notify_one();
+    return id;
+}
+
+int32_t uastar_serve_poll(uastar_engine *eng, uastar_serve_completion *out, int32_t cap) {
+    if (!eng || !eng->serve || (!out && cap > 0)) return -UASTAR_BAD_INPUT;
+    ServeState *S = eng->serve;
+    std::lock_guard<std::mutex> lk(S->mu);
+    int32_t n = 0;
+    while (n < cap && !S->done.empty()) {
+        out[n++] = S->done.front();
+        S->done.pop_front();
+    }
+    return n;
+}
+
+int32_t uastar_serve_cancel(uastar_engine *eng, int64_t id) {
+    if (!eng || !eng->serve) return UASTAR_BAD_INPUT;
+    ServeState *S = eng->serve;
+    std::lock_guard<std::mutex> lk(S->mu);
+    for (size_t i = 0; i < S->incoming.size(); ++i)
+        if (S->incoming[i].id == id) {
+            ServeReq r = std::move(S->incoming[i]);
+            S->incoming.erase(S->incoming.begin() + i);
+            uastar_serve_completion c;
+            std::memset(&c, 0, sizeof c);
+            c.id = id;
+            c.result.status = UASTAR_CANCELLED;
+            S->done.push_back(c);
+            S->outstanding -= 1;
+            S->stats.completed += 1;
+            S->stats.cancelled += 1;
+            return UASTAR_OK;
+        }
+    S->cancels.push_back(id);
+    S->cv.notify_one();
+    return UASTAR_OK;
+}
+
+int32_t uastar_serve_stop(uastar_engine *eng, double timeout_s, uastar_serve_stats *stats) {
+    if (!eng || !eng->serve) return UASTAR_BAD_INPUT;
+    ServeState *S = eng->serve;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->draining = true;
+        if (!(timeout_s > 0)) S->abort_now = true;
+        S->cv.notify_one();
+    }
+    if (timeout_s > 0) {
+        const double deadline = uastar_now_s() + timeout_s;
+        for (;;) {
+            {
+                std::lock_guard<std::mutex> lk(S->mu);
+                if (S->outstanding == 0) break;
+            }
+            if (uastar_now_s() > deadline) {
+                std::lock_guard<std::mutex> lk(S->mu);
+                S->abort_now = true;
+                S->cv.notify_one();
+                break;
+            }
+            std::this_thread::sleep_for(std::chrono::milliseconds(1));
+        }
+    }
+    if (S->th.joinable()) S->th.join();
+    const int32_t rc = S->loop_error;
+    if (stats) *stats = S->stats;
+    cudaStreamSynchronize(S->stream);
+    for (DevBuf *b : {&S->tab, &S->bitmaps, &S->heaps, &S->hsize, &S->cand, &S->descs, &S->outs, &S->states,
+                      &S->walk})
+        b->release();
+    cudaEventDestroy(S->q0);
+    cudaEventDestroy(S->q1);
+    cudaStreamDestroy(S->stream);
+    delete S;
+    eng->serve = nullptr;
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,529 @@
+// Plain engine: one instance per persistent cooperative launch, the whole GPU
+// as one GA* team (k heaps = k threads), plus the C-ABI glue shared by all
+// engines.  The search kernel is ga_search<> (ga_search.cuh) on a GridTeam.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "engine_internal.h"
+#include "ga_device.cuh"
+#include "ga_problems.cuh"
+#include "ga_search.cuh"
+
+using namespace uastar;
+
+// ------------------------------------------------------------------ kernels ---
+namespace uastar {
+
+__global__ void k_fill_ff(uint4 *p, size_t n16) {
+    const uint4 v = make_uint4(~0u, ~0u, ~0u, ~0u);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n16;
+         i += (size_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+template <class P>
+__global__ void __launch_bounds__(256, 1) k_plain_search(P prob, SearchMem<typename P::Entry> m,
+                                                      TeamState *st, uint64_t timeout_ns) {
+    GridTeam team{st, 0u, timeout_ns};
+    ga_search<P>(prob, team, m, ~0ull);
+}
+
+// Walk the prev chain from the goal slot (one thread: a pointer chase).
+// Writes keys goal -> start; *len = count, or cap + 1 when truncated.
+__global__ void k_walk(const Slot *tab, uint32_t goal_slot, unsigned long long *keys,
+                       uint64_t cap, unsigned long long *len) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    uint32_t s = goal_slot;
+    uint64_t n = 0;
+    while (s != kNone && n < cap) {
+        keys[n++] = __ldcg(&tab[s].key);
+        s = __ldcg(&tab[s].prev);
+    }
+    *len = (s != kNone) ? cap + 1 : n;
+}
+
+int32_t fail_cuda(uastar_engine *eng, cudaError_t e, const char *what) {
+    eng->set_err(std::string(what) + ": " + cudaGetErrorString(e));
+    return UASTAR_CUDA_ERROR;
+}
+
+}  // namespace uastar
+
+namespace {
+
+inline uint32_t next_pow2_u32(uint32_t v) {
+    uint32_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+inline int ceil_log2_u64(uint64_t v) {
+    int l = 0;
+    while ((1ull << l) < v) ++l;
+    return l;
+}
+inline double now_ms() {
+    return std::chrono::duration<double, std::milli>(
+               std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+
+TeamState fresh_team_state() {
+    TeamState s;
+    std::memset(&s, 0, sizeof s);
+    s.round_min[0] = s.round_min[1] = kInfCost;
+    s.goal_best = kInfCost;
+    s.goal_slot = kNone;
+    s.status = ST_RUNNING;
+    return s;
+}
+
+int32_t fill_ff(uastar_engine *eng, void *p, size_t bytes) {
+    const size_t n16 = bytes / 16;
+    const int blocks = std::max(1, eng->sms * 8);
+    k_fill_ff<<<blocks, 256, 0, eng->stream>>>(static_cast<uint4 *>(p), n16);
+    eng->launches++;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? UASTAR_OK : fail_cuda(eng, e, "fill");
+}
+
+struct PlainOut {
+    TeamState st;
+    double kernel_ms;
+    uint64_t slots;
+};
+
+// Run one instance with the whole GPU as the team.  Grows the dedup table /
+// heaps and retries when they overflow and were auto-sized.
+template <class P>
+int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t stride_auto,
+                  PlainOut *out) {
+    using E = typename P::Entry;
+    const uastar_config &c = eng->cfg;
+    const uint32_t block = (uint32_t)c.block_threads;
+    const uint32_t nblocks = (uint32_t)((c.heaps + c.block_threads - 1) / c.block_threads);
+    const uint32_t k = nblocks * block;
+    int log2 = c.hash_log2_slots > 0 ? c.hash_log2_slots : log2_auto;
+    uint32_t stride = c.heap_capacity > 0 ? next_pow2_u32((uint32_t)c.heap_capacity + 1) : stride_auto;
+
+    int max_active = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_active, k_plain_search<P>,
+                                                                  (int)block, 0);
+    if (e != cudaSuccess) return fail_cuda(eng, e, "occupancy");
+    if ((uint64_t)max_active * eng->sms < nblocks) {
+        eng->set_err("heaps/block_threads exceed one co-resident wave of the GPU");
+        return UASTAR_BAD_INPUT;
+    }
+
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        const uint64_t slots = 1ull << log2;
+        const size_t tab_b = slots * sizeof(Slot);
+        const size_t heap_b = (size_t)k * stride * sizeof(E);
+        const size_t cand_b = (size_t)k * P::kMoves * sizeof(Cand);
+        if ((e = eng->tab.ensure(tab_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc table");
+        if ((e = eng->heaps.ensure(heap_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc heaps");
+        if ((e = eng->heap_size.ensure((size_t)k * 4)) != cudaSuccess) return fail_cuda(eng, e, "alloc heap sizes");
+        if ((e = eng->cand.ensure(cand_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc candidates");
+        if ((e = eng->team.ensure(sizeof(TeamState))) != cudaSuccess) return fail_cuda(eng, e, "alloc state");
+
+        int32_t rc = fill_ff(eng, eng->tab.p, tab_b);
+        if (rc) return rc;
+        if ((e = cudaMemsetAsync(eng->heap_size.p, 0, (size_t)k * 4, eng->stream)) != cudaSuccess)
+            return fail_cuda(eng, e, "memset");
+        TeamState init = fresh_team_state();
+        if ((e = cudaMemcpyAsync(eng->team.p, &init, sizeof init, cudaMemcpyHostToDevice, eng->stream)) !=
+            cudaSuccess)
+            return fail_cuda(eng, e, "state upload");
+
+        SearchMem<E> m;
+        m.tab = eng->tab.as<Slot>();
+        m.mask = slots - 1;
+        m.max_inserted = (uint64_t)((double)slots * c.max_load);
+        m.max_probe = 4096;
+        m.heaps = eng->heaps.as<E>();
+        m.stride = stride;
+        m.heap_size = eng->heap_size.as<uint32_t>();
+        m.cand = eng->cand.as<Cand>();
+        m.max_rounds = (uint64_t)c.max_rounds;
+        TeamState *st = eng->team.as<TeamState>();
+        uint64_t timeout_ns = (uint64_t)(c.wait_timeout_s * 1e9);
+        P pr = prob;
+        void *args[] = {&pr, &m, &st, &timeout_ns};
+        cudaEventRecord(eng->ev0, eng->stream);
+        e = cudaLaunchCooperativeKernel((const void *)k_plain_search<P>, dim3(nblocks), dim3(block),
+                                        args, 0, eng->stream);
+        if (e != cudaSuccess) return fail_cuda(eng, e, "cooperative launch");
+        eng->launches++;
+        cudaEventRecord(eng->ev1, eng->stream);
+        if ((e = cudaMemcpyAsync(&out->st, st, sizeof(TeamState), cudaMemcpyDeviceToHost, eng->stream)) !=
+            cudaSuccess)
+            return fail_cuda(eng, e, "state download");
+        if ((e = cudaStreamSynchronize(eng->stream)) != cudaSuccess) return fail_cuda(eng, e, "search");
+        float ms = 0;
+        cudaEventElapsedTime(&ms, eng->ev0, eng->ev1);
+        out->kernel_ms = ms;
+        out->slots = slots;
+
+        const uint32_t s = out->st.status;
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        if (s == ST_HASH_FULL && c.hash_log2_slots <= 0 && log2 < 31 &&
+            (slots * 4 * sizeof(Slot)) < free_b + eng->tab.bytes) {
+            log2 += 2;
+            continue;
+        }
+        if (s == ST_HEAP_OVERFLOW && c.heap_capacity <= 0 && stride < (1u << 18) &&
+            (size_t)k * stride * 4 * sizeof(E) < free_b + eng->heaps.bytes) {
+            stride *= 4;
+            continue;
+        }
+        break;
+    }
+    return UASTAR_OK;
+}
+
+int32_t walk_keys(uastar_engine *eng, uint32_t goal_slot, uint64_t cap, std::vector<uint64_t> *keys) {
+    cudaError_t e;
+    const size_t need = (size_t)cap * 8 + 64;
+    if ((e = eng->walk.ensure(need)) != cudaSuccess) return fail_cuda(eng, e, "alloc walk");
+    unsigned long long *d_keys = eng->walk.as<unsigned long long>();
+    unsigned long long *d_len = d_keys + cap;
+    k_walk<<<1, 32, 0, eng->stream>>>(eng->tab.as<Slot>(), goal_slot, d_keys, cap, d_len);
+    eng->launches++;
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(eng, e, "walk launch");
+    unsigned long long len = 0;
+    if ((e = cudaMemcpyAsync(&len, d_len, 8, cudaMemcpyDeviceToHost, eng->stream)) != cudaSuccess)
+        return fail_cuda(eng, e, "walk length");
+    if ((e = cudaStreamSynchronize(eng->stream)) != cudaSuccess) return fail_cuda(eng, e, "walk");
+    if (len > cap) {
+        eng->set_err("solution path longer than the walk buffer");
+        return UASTAR_ARENA_FULL;
+    }
+    keys->resize(len);
+    if (len && (e = cudaMemcpyAsync(keys->data(), d_keys, len * 8, cudaMemcpyDeviceToHost, eng->stream)) !=
+                   cudaSuccess)
+        return fail_cuda(eng, e, "walk keys");
+    if ((e = cudaStreamSynchronize(eng->stream)) != cudaSuccess) return fail_cuda(eng, e, "walk copy");
+    std::reverse(keys->begin(), keys->end());
+    return UASTAR_OK;
+}
+
+int32_t grid_load_impl(uastar_engine *eng, const uint64_t *words, int32_t H, int32_t W) {
+    if (!eng) return UASTAR_BAD_INPUT;
+    if (!words || H <= 0 || W <= 0 || (uint64_t)H * (uint64_t)W >= (1ull << 32)) {
+        eng->set_err("grid must be non-empty with H*W < 2^32 cells");
+        return UASTAR_BAD_INPUT;
+    }
+    const uint64_t cells = (uint64_t)H * W;
+    const size_t bytes = ((cells + 63) / 64) * 8;
+    cudaError_t e;
+    if ((e = eng->bitmap.ensure(bytes + 16)) != cudaSuccess) return fail_cuda(eng, e, "alloc bitmap");
+    if ((e = cudaMemcpyAsync(eng->bitmap.p, words, bytes, cudaMemcpyHostToDevice, eng->stream)) != cudaSuccess)
+        return fail_cuda(eng, e, "bitmap upload");
+    eng->gH = H;
+    eng->gW = W;
+    eng->grid_loaded = true;
+    return UASTAR_OK;
+}
+
+int32_t grid_solve_impl(uastar_engine *eng, const uint64_t *host_words, int32_t sx, int32_t sy,
+                        int32_t ex, int32_t ey, uastar_grid_result *out) {
+    const double t0 = now_ms();
+    std::memset(out, 0, sizeof(*out));
+    eng->last_ok = false;
+    eng->path_cached = false;
+    eng->last_kind = UASTAR_KIND_GRID;
+    if (!eng->grid_loaded) {
+        eng->set_err("no grid loaded");
+        return out->status = UASTAR_BAD_INPUT;
+    }
+    const int32_t H = eng->gH, W = eng->gW;
+    if (sx < 0 || sx >= H || sy < 0 || sy >= W || ex < 0 || ex >= H || ey < 0 || ey >= W) {
+        eng->set_err("start/goal out of range");
+        return out->status = UASTAR_BAD_INPUT;
+    }
+    GridProblem prob;
+    prob.bm = eng->bitmap.as<uint32_t>();
+    prob.H = H;
+    prob.W = W;
+    prob.sx = sx;
+    prob.sy = sy;
+    prob.ex = ex;
+    prob.ey = ey;
+    const uint64_t cells = (uint64_t)H * W;
+    const int log2_auto = std::min(28, std::max(16, ceil_log2_u64(cells) - 1));
+    const uint32_t per_heap = (uint32_t)std::min<uint64_t>(8192, std::max<uint64_t>(64, 4 * cells / eng->cfg.heaps));
+    PlainOut po;
+    int32_t rc = run_plain(eng, prob, log2_auto, next_pow2_u32(per_heap), &po);
+    if (rc) return out->status = rc;
+    const TeamState &st = po.st;
+    out->status = (int32_t)st.status;
+    out->expanded = (int64_t)st.expanded;
+    out->generated = (int64_t)st.generated;
+    out->pushed = (int64_t)st.pushed;
+    out->rounds = (int64_t)st.round;
+    out->table_used = (int64_t)st.inserted;
+    out->kernel_ms = po.kernel_ms;
+    if (st.status == ST_OK) {
+        out->straight = (int64_t)(st.goal_best >> 32);
+        out->diagonal = (int64_t)(st.goal_best & 0xffffffffu);
+        out->cost_exact = (double)out->straight + (double)out->diagonal * std::sqrt(2.0);
+        out->cost = (float)out->cost_exact;
+        eng->last_ok = true;
+        eng->last_goal_slot = st.goal_slot;
+        eng->lsx = sx;
+        eng->lsy = sy;
+        eng->lex = ex;
+        eng->ley = ey;
+        // Path: walk prev pointers on the device, re-validate on the host.
+        std::vector<uint64_t> keys;
+        const uint64_t cap = std::min<uint64_t>(cells + 1, 1ull << 26);
+        rc = walk_keys(eng, st.goal_slot, cap, &keys);
+        if (rc) return out->status = rc;
+        eng->path.assign(keys.size(), 0);
+        for (size_t i = 0; i < keys.size(); ++i) eng->path[i] = (int32_t)keys[i];
+        eng->path_cached = true;
+        out->path_len = (int64_t)keys.size();
+        if (host_words) {
+            int64_t a = 0, b = 0;
+            float fc = 0;
+            if (uastar_validate_grid_path(host_words, H, W, sx, sy, ex, ey, eng->path.data(),
+                                          (int64_t)eng->path.size(), &a, &b, &fc) != UASTAR_OK ||
+                a != out->straight || b != out->diagonal) {
+                eng->set_err("engine returned a path that fails host validation");
+                eng->last_ok = false;
+                return out->status = UASTAR_CUDA_ERROR;
+            }
+            out->cost = fc;
+        }
+    } else if (st.status == ST_RUNNING) {
+        eng->set_err("search kernel ended without a status");
+        out->status = UASTAR_CUDA_ERROR;
+    }
+    out->solve_ms = now_ms() - t0;
+    return out->status;
+}
+
+uint64_t pack_board(int n, const uint8_t *tiles) {
+    uint64_t k = 0;
+    for (int i = 0; i < n * n; ++i) k |= (uint64_t)(tiles[i] & 15) << (4 * i);
+    return k;
+}
+
+bool board_ok(int n, const uint8_t *tiles) {
+    int seen = 0;
+    for (int i = 0; i < n * n; ++i) {
+        if (tiles[i] >= n * n || (seen >> tiles[i] & 1)) return false;
+        seen |= 1 << tiles[i];
+    }
+    return true;
+}
+
+// Solvability: the goal has no inversions and the blank in row n-1.  A
+// horizontal move keeps the inversion parity; a vertical move changes it by
+// n-1 and moves the blank one row.  So a board is solvable iff inversions are
+// even (n odd), or inversions + blank row has the parity of n-1 (n even).
+bool board_solvable(int n, const uint8_t *tiles) {
+    int inv = 0, brow = 0;
+    for (int i = 0; i < n * n; ++i) {
+        if (!tiles[i]) {
+            brow = i / n;
+            continue;
+        }
+        for (int j = i + 1; j < n * n; ++j)
+            if (tiles[j] && tiles[j] < tiles[i]) ++inv;
+    }
+    if (n & 1) return (inv & 1) == 0;
+    return ((inv + brow) & 1) == ((n - 1) & 1);
+}
+
+template <int N>
+int32_t puzzle_solve_n(uastar_engine *eng, const uint8_t *tiles, uastar_puzzle_result *out,
+                       PlainOut *po) {
+    PuzzleProblem<N> prob;
+    prob.pdb = eng->pdb[N].as<uint8_t>();
+    prob.start = pack_board(N, tiles);
+    prob.goal = PuzzleProblem<N>::goal_key();
+    return run_plain(eng, prob, N == 3 ? 18 : 24, 1024, po);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI ---
+extern "C" {
+
+const char *uastar_build_info(void) {
+    return "uastar_gb300 GA* engine, built for sm_103a";
+}
+
+uastar_engine *uastar_create(int32_t ordinal, const uastar_config *cfg) {
+    auto *eng = new uastar_engine();
+    eng->device = ordinal;
+    if (cfg) eng->cfg = *cfg;
+    uastar_config &c = eng->cfg;
+    if (c.heaps <= 0) c.heaps = 8192;
+    if (c.block_threads <= 0) c.block_threads = 128;
+    c.block_threads = std::max(32, std::min(256, (c.block_threads + 31) / 32 * 32));
+    if (!(c.max_load > 0.0 && c.max_load < 1.0)) c.max_load = 0.9;
+    if (c.max_rounds <= 0) c.max_rounds = 1ll << 31;
+    if (!(c.wait_timeout_s > 0.0)) c.wait_timeout_s = 10.0;
+    cudaError_t e = cudaSetDevice(ordinal);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&eng->sms, cudaDevAttrMultiProcessorCount, ordinal);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&eng->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&eng->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&eng->ev1);
+    if (e != cudaSuccess) {
+        delete eng;
+        return nullptr;
+    }
+    eng->stream = eng->own_stream;
+    return eng;
+}
+
+void uastar_destroy(uastar_engine *eng) {
+    if (!eng) return;
+    if (eng->serve) uastar_serve_stop(eng, 0.0, nullptr);
+    cudaSetDevice(eng->device);
+    cudaStreamSynchronize(eng->stream);
+    for (DevBuf *b : {&eng->tab, &eng->heaps, &eng->heap_size, &eng->cand, &eng->team, &eng->walk,
+                      &eng->bitmap, &eng->b_desc, &eng->b_out, &eng->b_queue, &eng->b_bitmaps,
+                      &eng->b_tab, &eng->b_heaps, &eng->b_hsize, &eng->b_cand, &eng->b_walk,
+                      &eng->b_walklen})
+        b->release();
+    for (auto &b : eng->pdb) b.release();
+    if (eng->ev0) cudaEventDestroy(eng->ev0);
+    if (eng->ev1) cudaEventDestroy(eng->ev1);
+    if (eng->own_stream) cudaStreamDestroy(eng->own_stream);
+    delete eng;
+}
+
+const char *uastar_last_error(const uastar_engine *eng) { return eng ? eng->err.c_str() : "null engine"; }
+
+int32_t uastar_set_stream(uastar_engine *eng, void *cuda_stream) {
+    if (!eng) return UASTAR_BAD_INPUT;
+    eng->stream = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : eng->own_stream;
+    return UASTAR_OK;
+}
+
+int64_t uastar_kernel_launches(const uastar_engine *eng) { return eng ? eng->launches.load() : 0; }
+
+int32_t uastar_grid_load(uastar_engine *eng, const uint64_t *words, int32_t H, int32_t W) {
+    if (!eng) return UASTAR_BAD_INPUT;
+    cudaSetDevice(eng->device);
+    int32_t rc = grid_load_impl(eng, words, H, W);
+    if (rc) return rc;
+    cudaError_t e = cudaStreamSynchronize(eng->stream);
+    return e == cudaSuccess ? UASTAR_OK : fail_cuda(eng, e, "bitmap upload");
+}
+
+int32_t uastar_grid_solve_loaded(uastar_engine *eng, int32_t sx, int32_t sy, int32_t ex, int32_t ey,
+                                 uastar_grid_result *out) {
+    if (!eng || !out) return UASTAR_BAD_INPUT;
+    cudaSetDevice(eng->device);
+    return grid_solve_impl(eng, nullptr, sx, sy, ex, ey, out);
+}
+
+int32_t uastar_grid_solve(uastar_engine *eng, const uint64_t *words, int32_t H, int32_t W, int32_t sx,
+                          int32_t sy, int32_t ex, int32_t ey, uastar_grid_result *out) {
+    if (!eng || !out) return UASTAR_BAD_INPUT;
+    cudaSetDevice(eng->device);
+    const double t0 = now_ms();
+    int32_t rc = grid_load_impl(eng, words, H, W);
+    if (rc) {
+        std::memset(out, 0, sizeof(*out));
+        return out->status = rc;
+    }
+    rc = grid_solve_impl(eng, words, sx, sy, ex, ey, out);
+    out->solve_ms = now_ms() - t0;
+    return rc;
+}
+
+int64_t uastar_grid_path(uastar_engine *eng, int32_t *ids, int64_t cap) {
+    if (!eng) return -UASTAR_BAD_INPUT;
+    if (eng->last_kind != UASTAR_KIND_GRID || !eng->last_ok || !eng->path_cached) return -UASTAR_NO_SOLUTION;
+    const int64_t n = (int64_t)eng->path.size();
+    if (ids)
+        for (int64_t i = 0; i < n && i < cap; ++i) ids[i] = eng->path[i];
+    return n;
+}
+
+int32_t uastar_puzzle_solve(uastar_engine *eng, int32_t n, const uint8_t *tiles, uastar_puzzle_result *out) {
+    if (!eng || !out) return UASTAR_BAD_INPUT;
+    const double t0 = now_ms();
+    std::memset(out, 0, sizeof(*out));
+    cudaSetDevice(eng->device);
+    eng->last_ok = false;
+    eng->path_cached = false;
+    eng->last_kind = UASTAR_KIND_PUZZLE;
+    if ((n != 3 && n != 4) || !tiles || !board_ok(n, tiles)) {
+        eng->set_err("puzzle must be 3x3 or 4x4 with tiles 0..n*n-1 once each");
+        return out->status = UASTAR_BAD_INPUT;
+    }
+    if (!eng->pdb_ready[n]) {
+        eng->set_err("pattern database not resident: call uastar_pdb_build or uastar_pdb_load");
+        return out->status = UASTAR_BAD_INPUT;
+    }
+    if (!board_solvable(n, tiles)) {
+        out->status = UASTAR_NO_SOLUTION;
+        out->solve_ms = now_ms() - t0;
+        return out->status;
+    }
+    PlainOut po;
+    int32_t rc = n == 3 ? puzzle_solve_n<3>(eng, tiles, out, &po) : puzzle_solve_n<4>(eng, tiles, out, &po);
+    if (rc) return out->status = rc;
+    const TeamState &st = po.st;
+    out->status = (int32_t)st.status;
+    out->expanded = (int64_t)st.expanded;
+    out->generated = (int64_t)st.generated;
+    out->pushed = (int64_t)st.pushed;
+    out->rounds = (int64_t)st.round;
+    out->table_used = (int64_t)st.inserted;
+    out->kernel_ms = po.kernel_ms;
+    if (st.status == ST_OK) {
+        out->steps = (int32_t)st.goal_best;
+        std::vector<uint64_t> keys;
+        rc = walk_keys(eng, st.goal_slot, 4096, &keys);
+        if (rc) return out->status = rc;
+        eng->path.clear();
+        for (size_t i = 1; i < keys.size(); ++i) {
+            auto blank = [n](uint64_t k) {
+                for (int c = 0; c < n * n; ++c)
+                    if (((k >> (4 * c)) & 15) == 0) return c;
+                return -1;
+            };
+            const int pb = blank(keys[i - 1]), cb = blank(keys[i]);
+            const int d = cb - pb == n ? 0 : cb - pb == -n ? 1 : cb - pb == 1 ? 2 : 3;
+            eng->path.push_back(d);
+        }
+        if ((int64_t)eng->path.size() != out->steps ||
+            uastar_validate_puzzle_moves(n, tiles, eng->path.data(), (int64_t)eng->path.size()) != UASTAR_OK) {
+            eng->set_err("engine returned moves that fail host validation");
+            return out->status = UASTAR_CUDA_ERROR;
+        }
+        eng->last_ok = true;
+        eng->path_cached = true;
+        eng->last_n = n;
+        std::memcpy(eng->last_tiles, tiles, (size_t)n * n);
+    } else if (st.status == ST_RUNNING) {
+        eng->set_err("search kernel ended without a status");
+        out->status = UASTAR_CUDA_ERROR;
+    }
+    out->solve_ms = now_ms() - t0;
+    return out->status;
+}
+
+int64_t uastar_puzzle_moves(uastar_engine *eng, int32_t *moves, int64_t cap) {
+    if (!eng) return -UASTAR_BAD_INPUT;
+    if (eng->last_kind != UASTAR_KIND_PUZZLE || !eng->last_ok || !eng->path_cached) return -UASTAR_NO_SOLUTION;
+    const int64_t n = (int64_t)eng->path.size();
+    if (moves)
+        for (int64_t i = 0; i < n && i < cap; ++i) moves[i] = eng->path[i];
+    return n;
+}
+
+}  // extern "C"

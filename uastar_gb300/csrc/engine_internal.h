@@ -1,0 +1,88 @@
+// Host-side engine object shared by the engine's translation units
+// (engine.cu: plain solves; pdb.cu: pattern databases; batch.cu: batched
+// and serving engines).  Not part of the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <condition_variable>
+#include <cstdint>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/uastar_gpu.h"
+
+namespace uastar {
+
+// Grow-only device allocation.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need) {
+        if (need <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, need);
+        if (e == cudaSuccess) bytes = need;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+struct ServeState;  // batch.cu
+
+}  // namespace uastar
+
+struct uastar_engine {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    uastar_config cfg{};
+    int sms = 0;
+    std::string err;
+    std::atomic<int64_t> launches{0};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    // plain engine buffers
+    uastar::DevBuf tab, heaps, heap_size, cand, team, walk, bitmap;
+    int32_t gH = 0, gW = 0;
+    bool grid_loaded = false;
+    // pattern databases, indexed by board side
+    uastar::DevBuf pdb[5];
+    bool pdb_ready[5] = {false, false, false, false, false};
+
+    // last plain solve
+    int last_kind = 0;          // UASTAR_KIND_GRID / UASTAR_KIND_PUZZLE
+    bool last_ok = false;
+    uint32_t last_goal_slot = 0;
+    int32_t lsx = 0, lsy = 0, lex = 0, ley = 0;
+    int32_t last_n = 0;
+    uint8_t last_tiles[16] = {0};
+    bool path_cached = false;
+    std::vector<int32_t> path;  // grid: cell ids; puzzle: moves
+
+    // batched / serving engines
+    uastar::DevBuf b_desc, b_out, b_queue, b_bitmaps, b_tab, b_heaps, b_hsize, b_cand, b_walk,
+        b_walklen;
+    uastar::ServeState *serve = nullptr;  // owned; released by uastar_serve_stop
+
+    void set_err(const std::string &s) { err = s; }
+};
+
+namespace uastar {
+// engine.cu
+int32_t fail_cuda(uastar_engine *eng, cudaError_t e, const char *what);
+// pdb.cu
+int32_t pdb_build_device(uastar_engine *eng, int n, double *ms);
+}  // namespace uastar

@@ -1,0 +1,186 @@
+// Device-side building blocks of the GA* engine (sm_103a):
+//   - the dedup-table slot and successor-candidate records,
+//   - the per-search team state,
+//   - L2-coherent loads, 64-bit hashing, open-addressed find-or-insert with
+//     atomicCAS, CAS-based minimum of a cost word,
+//   - a grid-wide barrier whose every wait is bounded in time.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace uastar {
+
+constexpr uint64_t kEmptyKey = ~0ull;   // free dedup slot (no valid state packs to all ones)
+constexpr uint64_t kInfCost = ~0ull;    // "no cost yet"
+constexpr uint32_t kNone = 0xFFFFFFFFu; // null slot index
+constexpr unsigned kFull = 0xFFFFFFFFu; // full warp mask
+
+// Status codes (mirror UASTAR_* in include/uastar_gpu.h).
+enum : uint32_t {
+    ST_OK = 0,
+    ST_NO_SOLUTION = 1,
+    ST_HEAP_OVERFLOW = 2,
+    ST_ARENA_FULL = 3,
+    ST_HASH_FULL = 4,
+    ST_ITER_LIMIT = 5,
+    ST_CUDA_ERROR = 6,
+    ST_BAD_INPUT = 7,
+    ST_TIMEOUT = 8,
+    ST_RUNNING = 9,
+};
+
+// One dedup-table slot: exactly one 32-byte sector, so a probe, the g update
+// and the pop-time read of a node each touch a single sector.
+struct __align__(32) Slot {
+    unsigned long long key;  // state key (grid cell id / packed board); kEmptyKey = free
+    unsigned long long g;    // cost from the start (problem-specific packing)
+    uint32_t aux;            // problem data (puzzle: PDB parts and last move)
+    uint32_t prev;           // parent slot, kNone for the root
+    uint32_t pad0, pad1;
+};
+static_assert(sizeof(Slot) == 32, "slot must be one sector");
+
+// A successor whose g strictly improved its slot this round.
+struct __align__(16) Cand {
+    uint32_t slot;
+    uint32_t parent;
+    unsigned long long g;
+    unsigned long long f;
+    uint32_t aux;
+    uint32_t pad;
+};
+static_assert(sizeof(Cand) == 32, "candidate record");
+
+// Search state shared by the threads of one GA* team (the whole grid for the
+// plain engine, one CTA for the batched engine).  Round-indexed fields are
+// double-buffered by round parity so that they can be reset one round ahead
+// without a third barrier.
+struct __align__(16) TeamState {
+    unsigned long long round_min[2];  // min popped f of the round (cost word)
+    unsigned long long goal_best;     // best goal f popped so far
+    unsigned long long round;         // rounds completed
+    unsigned long long inserted;      // dedup slots in use
+    unsigned long long expanded, generated, pushed;
+    uint32_t cand_count[2];           // candidates appended this round
+    uint32_t goal_slot;
+    uint32_t error;                   // first error of phase 1 / barriers (0 = none)
+    uint32_t error2[2];               // first error of phase 2, by round parity
+    uint32_t status;                  // final status (ST_RUNNING while active)
+    uint32_t base;                    // heap rotation for pushes
+    uint32_t started;                 // start node seeded
+    uint32_t barrier;                 // grid-barrier arrival counter
+    uint32_t pad_;
+};
+
+// ---------------------------------------------------------------- loads ---
+// Cross-SM mutable data is read through L2 (ld.global.cg): L1 is not coherent
+// across SMs, and the table, heaps and candidates move between SMs every round.
+__device__ __forceinline__ unsigned long long ldcg_u64(const unsigned long long *p) {
+    return __ldcg(p);
+}
+__device__ __forceinline__ uint32_t ldcg_u32(const uint32_t *p) { return __ldcg(p); }
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void set_error(uint32_t *err, uint32_t code) {
+    atomicCAS(err, 0u, code);
+}
+
+// ------------------------------------------------------------- hashing ---
+// 64-bit finalizer of MurmurHash3 (Appleby, public domain): a bijective mix
+// whose low bits depend on every key bit.
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return k;
+}
+
+enum : int { FIND_FOUND = 0, FIND_INSERTED = 1, FIND_FULL = 2 };
+
+// Open addressing with linear probing over 32-byte slots.  A free slot is
+// claimed with atomicCAS on its key; the winner of the race owns it and every
+// other writer of the same key sees the key on its retry.
+__device__ __forceinline__ int find_or_insert(Slot *tab, uint64_t mask, uint64_t key,
+                                              uint32_t max_probe, uint32_t *slot_out) {
+    uint64_t h = mix64(key) & mask;
+    for (uint32_t i = 0; i < max_probe; ++i) {
+        unsigned long long k = ldcg_u64(&tab[h].key);
+        if (k == key) {
+            *slot_out = (uint32_t)h;
+            return FIND_FOUND;
+        }
+        if (k == kEmptyKey) {
+            unsigned long long old = atomicCAS(&tab[h].key, kEmptyKey, (unsigned long long)key);
+            if (old == kEmptyKey) {
+                *slot_out = (uint32_t)h;
+                return FIND_INSERTED;
+            }
+            if (old == key) {
+                *slot_out = (uint32_t)h;
+                return FIND_FOUND;
+            }
+        }
+        h = (h + 1) & mask;
+    }
+    return FIND_FULL;
+}
+
+// ------------------------------------------------------- warp helpers ---
+__device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
+    return __shfl_sync(kFull, (unsigned long long)v, src);
+}
+__device__ __forceinline__ uint64_t shfl_xor64(uint64_t v, int m) {
+    return __shfl_xor_sync(kFull, (unsigned long long)v, m);
+}
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// ------------------------------------------------------------- barrier ---
+// Grid-wide barrier for a cooperative launch.  The arrival counter only grows
+// (one atomicAdd per CTA per barrier, no reset), so barrier number e is
+// complete when the counter reaches e * nblocks (compared modulo 2^32).
+// Thread 0 of each CTA waits with a time bound: when it expires, or when
+// another CTA has flagged an error, it records ST_TIMEOUT (first error wins)
+// and leaves; the caller checks the error word after every barrier, so all
+// CTAs stop together at the next one.
+__device__ __forceinline__ void grid_barrier(uint32_t *counter, uint32_t nblocks, uint32_t &epoch,
+                                             uint32_t *err, uint64_t timeout_ns) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        epoch += 1;
+        const uint32_t target = epoch * nblocks;
+        __threadfence();
+        atomicAdd(counter, 1u);
+        const uint64_t t0 = globaltimer_ns();
+        uint32_t spins = 0;
+        while ((int32_t)(ld_acquire_u32(counter) - target) < 0) {
+            if ((++spins & 63u) == 0) {
+                if (ldcg_u32(err) != 0) break;
+                if (globaltimer_ns() - t0 > timeout_ns) {
+                    set_error(err, ST_TIMEOUT);
+                    break;
+                }
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+}  // namespace uastar

@@ -1,0 +1,305 @@
+// The two search problems the engine instantiates GA* for.
+//
+// A problem supplies: the heap entry type and its order, the cost word
+// (compared with cost_cmp), the start/goal keys, f = g + h, the valid-move
+// mask of a popped node and the successor of one move.
+//
+// GridProblem   — 8-direction grid of uAstar's --pathway mode.  Costs are the
+//                 exact pair (straight A, diagonal B) with value A + B*sqrt(2),
+//                 packed A<<32 | B and compared with integer arithmetic only,
+//                 so the search is exact where the reference accumulates float32.
+// PuzzleProblem — n x n sliding tile of --puzzle with the additive disjoint
+//                 pattern database; integer move counts.
+#pragma once
+#include <cstdint>
+
+#include "ga_device.cuh"
+
+namespace uastar {
+
+// ----------------------------------------------------------------- grid ---
+struct __align__(16) GridEntry {
+    uint32_t fa, fb;  // f = fa + fb*sqrt(2)
+    uint32_t slot;
+    uint32_t tie;     // ~ h scaled by 1024: among equal f, smaller h (deeper) first
+};
+
+// sign((a1 + b1*sqrt2) - (a2 + b2*sqrt2)) for packed a<<32|b words; kInfCost
+// is larger than every cost.  Exact for a, b < 2^31.
+__host__ __device__ __forceinline__ int grid_cost_cmp(uint64_t p, uint64_t q) {
+    if (p == q) return 0;
+    if (p == kInfCost) return 1;
+    if (q == kInfCost) return -1;
+    const int64_t d = (int64_t)(p >> 32) - (int64_t)(q >> 32);            // straight diff
+    const int64_t e = (int64_t)(q & 0xffffffffu) - (int64_t)(p & 0xffffffffu);  // value = d - e*sqrt2
+    if (e == 0) return d > 0 ? 1 : (d < 0 ? -1 : 0);
+    if (d >= 0 && e < 0) return 1;
+    if (d <= 0 && e > 0) return -1;
+    const uint64_t lhs = (uint64_t)(d * d), rhs = (uint64_t)(2 * e * e);
+    const int s = lhs > rhs ? 1 : -1;  // never equal: sqrt(2) is irrational
+    return d > 0 ? s : -s;
+}
+
+struct GridProblem {
+    using Entry = GridEntry;
+    static constexpr int kMoves = 8;
+
+    const uint32_t *bm;  // bitmap as 32-bit words (same bytes as the uint64 words)
+    int32_t H, W;
+    int32_t sx, sy, ex, ey;
+
+    __device__ static int cost_cmp(uint64_t a, uint64_t b) { return grid_cost_cmp(a, b); }
+
+    __device__ __forceinline__ bool open(int64_t id) const {
+        return (__ldg(bm + (id >> 5)) >> (id & 31)) & 1u;
+    }
+    __device__ uint64_t start_key() const { return (uint64_t)sx * W + sy; }
+    __device__ uint32_t start_aux() const { return 0; }
+    __device__ bool is_goal(uint64_t key) const { return key == (uint64_t)ex * W + ey; }
+
+    // Octile heuristic (src/pathway/CPU-solver.cpp:139-146): with dx, dy the
+    // distances to the goal, h = min(dx,dy)*sqrt2 + |dx-dy| — as a pair.
+    __device__ __forceinline__ uint64_t h_of(uint64_t key) const {
+        const uint32_t c = (uint32_t)key;  // H*W < 2^32 is checked on the host
+        const int x = (int)(c / (uint32_t)W), y = (int)(c - (uint32_t)x * (uint32_t)W);
+        const int dx = abs(x - ex), dy = abs(y - ey);
+        const int mn = min(dx, dy), mx = max(dx, dy);
+        return ((uint64_t)(mx - mn) << 32) | (uint64_t)mn;
+    }
+    __device__ __forceinline__ uint64_t f_of(uint64_t key, uint64_t g, uint32_t) const {
+        return g + h_of(key);  // field-wise: both halves stay below 2^31
+    }
+
+    // Valid moves of a popped cell, bit i = direction i (4 straight, then 4
+    // diagonal; src/utils.hpp:120-122).  Only an open cell moves
+    // (CPU-solver.cpp:98-100).  A move into a blocked cell is legal in the
+    // reference but such a cell has no out-moves, so it is generated only
+    // when it is the goal: no path cost changes.
+    __device__ uint32_t moves(uint64_t key, uint32_t) const {
+        const uint32_t c = (uint32_t)key;
+        const int x = (int)(c / (uint32_t)W), y = (int)(c - (uint32_t)x * (uint32_t)W);
+        if (!open((int64_t)key)) return 0;
+        const int gx = ex, gy = ey;
+        uint32_t m = 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int nx = x + c_dx(i), ny = y + c_dy(i);
+            if (nx < 0 || nx >= H || ny < 0 || ny >= W) continue;
+            const int64_t nid = (int64_t)nx * W + ny;
+            if (open(nid) || (nx == gx && ny == gy)) m |= 1u << i;
+        }
+        return m;
+    }
+    __device__ __forceinline__ static int c_dx(int i) {
+        return i == 0 ? 1 : i == 1 ? -1 : i < 4 ? 0 : (i < 6 ? 1 : -1);
+    }
+    __device__ __forceinline__ static int c_dy(int i) {
+        return i < 2 ? 0 : i == 2 ? 1 : i == 3 ? -1 : ((i & 1) ? -1 : 1);
+    }
+    __device__ void apply(uint64_t key, uint64_t g, uint32_t, int mv, uint64_t &nkey,
+                          uint64_t &ng, uint32_t &naux, uint64_t &nf) const {
+        const uint32_t c = (uint32_t)key;
+        const int x = (int)(c / (uint32_t)W), y = (int)(c - (uint32_t)x * (uint32_t)W);
+        nkey = (uint64_t)(x + c_dx(mv)) * W + (uint64_t)(y + c_dy(mv));
+        ng = g + (mv < 4 ? (1ull << 32) : 1ull);
+        naux = 0;
+        nf = ng + h_of(nkey);
+    }
+    __device__ __forceinline__ Entry make_entry(uint64_t f, uint64_t g, uint32_t slot) const {
+        Entry e;
+        e.fa = (uint32_t)(f >> 32);
+        e.fb = (uint32_t)f;
+        e.slot = slot;
+        const uint64_t ha = (f >> 32) - (g >> 32), hb = (f & 0xffffffffu) - (g & 0xffffffffu);
+        const uint64_t t = ha * 1024 + hb * 1448;
+        e.tie = t > 0xffffffffull ? 0xffffffffu : (uint32_t)t;
+        return e;
+    }
+    __device__ __forceinline__ static uint64_t entry_cost(const Entry &e) {
+        return ((uint64_t)e.fa << 32) | e.fb;
+    }
+    __device__ __forceinline__ static bool less(const Entry &a, const Entry &b) {
+        const int c = grid_cost_cmp(entry_cost(a), entry_cost(b));
+        return c < 0 || (c == 0 && a.tie < b.tie);
+    }
+    __device__ __forceinline__ static Entry load(const Entry *p) {
+        const uint4 u = __ldcg(reinterpret_cast<const uint4 *>(p));
+        Entry e;
+        e.fa = u.x;
+        e.fb = u.y;
+        e.slot = u.z;
+        e.tie = u.w;
+        return e;
+    }
+    __device__ __forceinline__ static void store(Entry *p, const Entry &e) {
+        *reinterpret_cast<uint4 *>(p) = make_uint4(e.fa, e.fb, e.slot, e.tie);
+    }
+    // Node record fields needed at pop time: key and g share the first 16 B.
+    __device__ __forceinline__ static void load_node(const Slot *s, uint64_t &key, uint64_t &g,
+                                                     uint32_t &aux) {
+        const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(s));
+        key = v.x;
+        g = v.y;
+        aux = 0;
+    }
+};
+
+// --------------------------------------------------------------- puzzle ---
+struct __align__(8) PuzzleEntry {
+    uint32_t key;   // f << 16 | (0xFFFF - g): min f, then max g
+    uint32_t slot;
+};
+
+// Disjoint pattern partitions of the reference (src/puzzle/CPU-solver.hpp:43-70)
+// and the mixed-radix multipliers of its rank (src/puzzle/database.cpp:8-25):
+// multiple[j] = prod_{i=j}^{k-1} (n*n - i), rank = sum_j v_j * multiple[j+1],
+// v_j = cell of tracked tile j minus the number of earlier tracked tiles on
+// lower cells (database.cpp:140-163).
+template <int N> struct PuzzlePatterns;
+template <> struct PuzzlePatterns<3> {
+    static constexpr int kNum = 1;
+    __host__ __device__ static constexpr int count(int) { return 8; }
+    __host__ __device__ static constexpr int tile(int, int j) { return j + 1; }
+    __host__ __device__ static constexpr uint64_t offset(int) { return 0; }
+};
+template <> struct PuzzlePatterns<4> {
+    static constexpr int kNum = 2;
+    __host__ __device__ static constexpr int count(int p) { return p == 0 ? 8 : 7; }
+    __host__ __device__ static constexpr int tile(int p, int j) {
+        return p == 0 ? (j < 6 ? j + 1 : (j == 6 ? 9 : 13))
+                      : (j < 2 ? j + 7 : (j < 5 ? j + 8 : j + 9));
+    }
+    __host__ __device__ static constexpr uint64_t offset(int p) { return p == 0 ? 0ull : 518918400ull; }
+};
+
+template <int N> __host__ __device__ constexpr uint32_t pattern_mult(int p, int j) {
+    // prod_{i=j}^{k-1} (N*N - i)
+    uint32_t m = 1;
+    for (int i = j; i < PuzzlePatterns<N>::count(p); ++i) m *= (uint32_t)(N * N - i);
+    return m;
+}
+template <int N> __host__ __device__ constexpr int pattern_of_tile(int t) {
+    for (int p = 0; p < PuzzlePatterns<N>::kNum; ++p)
+        for (int j = 0; j < PuzzlePatterns<N>::count(p); ++j)
+            if (PuzzlePatterns<N>::tile(p, j) == t) return p;
+    return -1;
+}
+
+template <int N> struct PuzzleProblem {
+    using Entry = PuzzleEntry;
+    static constexpr int kMoves = 4;
+    static constexpr int NN = N * N;
+
+    const uint8_t *pdb;   // concatenated tables
+    uint64_t start;       // packed board: cell i at bits 4i
+    uint64_t goal;
+
+    __device__ static int cost_cmp(uint64_t a, uint64_t b) { return a < b ? -1 : (a > b ? 1 : 0); }
+
+    __host__ __device__ static uint64_t goal_key() {
+        uint64_t k = 0;
+        for (int i = 0; i < NN; ++i) k |= (uint64_t)((i + 1) % NN) << (4 * i);
+        return k;
+    }
+    // Inverse permutation: nibble t = cell of tile t.
+    __device__ __forceinline__ static uint64_t inverse(uint64_t key) {
+        uint64_t inv = 0;
+#pragma unroll
+        for (int i = 0; i < NN; ++i) inv |= (uint64_t)i << (4 * ((key >> (4 * i)) & 15));
+        return inv;
+    }
+    template <int P> __device__ __forceinline__ static uint32_t rank(uint64_t inv) {
+        uint32_t used = 0, code = 0;
+#pragma unroll
+        for (int j = 0; j < PuzzlePatterns<N>::count(P); ++j) {
+            const uint32_t pos = (uint32_t)(inv >> (4 * PuzzlePatterns<N>::tile(P, j))) & 15u;
+            const uint32_t v = pos - __popc(used & ((1u << pos) - 1u));
+            code += v * pattern_mult<N>(P, j + 1);
+            used |= 1u << pos;
+        }
+        return code;
+    }
+    __device__ __forceinline__ uint32_t part(int p, uint64_t inv) const {
+        if (p == 0) return __ldg(pdb + PuzzlePatterns<N>::offset(0) + rank<0>(inv));
+        if constexpr (PuzzlePatterns<N>::kNum > 1)
+            return __ldg(pdb + PuzzlePatterns<N>::offset(1) + rank<1>(inv));
+        return 0;
+    }
+    // aux = part0 | part1 << 8 | (last move + 1) << 16
+    __device__ static uint32_t hsum(uint32_t aux) { return (aux & 0xff) + ((aux >> 8) & 0xff); }
+
+    __device__ uint64_t start_key() const { return start; }
+    __device__ uint32_t start_aux() const {
+        const uint64_t inv = inverse(start);
+        uint32_t a = part(0, inv);
+        if (PuzzlePatterns<N>::kNum > 1) a |= part(1, inv) << 8;
+        return a;
+    }
+    __device__ bool is_goal(uint64_t key) const { return key == goal; }
+    __device__ __forceinline__ uint64_t f_of(uint64_t, uint64_t g, uint32_t aux) const {
+        return g + hsum(aux);
+    }
+    __device__ __forceinline__ static int blank(uint64_t key) {
+        constexpr uint64_t kPad = NN < 16 ? (~0ull << (4 * (NN < 16 ? NN : 0))) : 0ull;
+        uint64_t z = ~(key | kPad);
+        z = z & (z >> 1) & (z >> 2) & (z >> 3) & 0x1111111111111111ull;
+        return (__ffsll((long long)z) - 1) >> 2;
+    }
+    // Blank moves 0..3 = DX/DY[0..3] of src/utils.hpp:120-121.  The move that
+    // would undo the parent's move is skipped: it leads back to the parent,
+    // whose g is already lower, so it never improves a slot.
+    __device__ uint32_t moves(uint64_t key, uint32_t aux) const {
+        const int b = blank(key), bx = b / N, by = b % N;
+        uint32_t m = 0;
+        if (bx + 1 < N) m |= 1u;
+        if (bx > 0) m |= 2u;
+        if (by + 1 < N) m |= 4u;
+        if (by > 0) m |= 8u;
+        const uint32_t last = aux >> 16;
+        if (last) m &= ~(1u << ((last - 1) ^ 1));
+        return m;
+    }
+    __device__ void apply(uint64_t key, uint64_t g, uint32_t aux, int mv, uint64_t &nkey,
+                          uint64_t &ng, uint32_t &naux, uint64_t &nf) const {
+        const int b = blank(key);
+        const int q = b + (mv == 0 ? N : mv == 1 ? -N : mv == 2 ? 1 : -1);
+        const uint64_t t = (key >> (4 * q)) & 15;
+        nkey = (key & ~(15ull << (4 * q))) | (t << (4 * b));
+        const uint64_t inv = inverse(nkey);
+        uint32_t a = aux & 0xffffu;
+        if (pattern_of_tile<N>((int)t) == 0)
+            a = (a & 0xff00u) | part(0, inv);
+        else
+            a = (a & 0x00ffu) | (part(1, inv) << 8);
+        naux = a | ((uint32_t)(mv + 1) << 16);
+        ng = g + 1;
+        nf = ng + hsum(naux);
+    }
+    __device__ __forceinline__ Entry make_entry(uint64_t f, uint64_t g, uint32_t slot) const {
+        Entry e;
+        e.key = ((uint32_t)f << 16) | (0xffffu - (uint32_t)g);
+        e.slot = slot;
+        return e;
+    }
+    __device__ __forceinline__ static uint64_t entry_cost(const Entry &e) { return e.key >> 16; }
+    __device__ __forceinline__ static bool less(const Entry &a, const Entry &b) { return a.key < b.key; }
+    __device__ __forceinline__ static Entry load(const Entry *p) {
+        const uint2 u = __ldcg(reinterpret_cast<const uint2 *>(p));
+        Entry e;
+        e.key = u.x;
+        e.slot = u.y;
+        return e;
+    }
+    __device__ __forceinline__ static void store(Entry *p, const Entry &e) {
+        *reinterpret_cast<uint2 *>(p) = make_uint2(e.key, e.slot);
+    }
+    __device__ __forceinline__ static void load_node(const Slot *s, uint64_t &key, uint64_t &g,
+                                                     uint32_t &aux) {
+        const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(s));
+        key = v.x;
+        g = v.y;
+        aux = __ldcg(&s->aux);
+    }
+};
+
+}  // namespace uastar
