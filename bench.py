@@ -118,7 +118,7 @@ def run_ours(args, rank, world, local_rank):
     pinned.numpy().view(np.uint64)[:] = words
     host_words = pinned.numpy().view(np.uint64)
 
-    eng = Engine(local_rank, heaps=8192, block_threads=128, hash_log2_slots=28)
+    eng = Engine(local_rank, heaps=8192, block_threads=256, threads_per_heap=4, hash_log2_slots=28)
     eng.set_stream(stream.cuda_stream)
     eng.grid_load(words, sp.H, sp.W)
 
@@ -195,7 +195,7 @@ def run_ours(args, rank, world, local_rank):
         "warmup": args.warmup, "ms_per_step": round(elapsed_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic (seeded generator)",
         "config": {"workload": WORKLOAD, "grid": "20000x20000", "block_rate": 0.30, "seed": sp.seed,
-                   "heaps": 8192, "block_threads": 128, "hash_slots": 2 ** 28,
+                   "heaps": 8192, "block_threads": 256, "threads_per_heap": 4, "hash_slots": 2 ** 28,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2: each solve rewrites its 8.6 GB dedup table first",
                    "step": "one full solve (search + path walk + host validation), bitmap resident"},

@@ -58,12 +58,14 @@ typedef struct uastar_engine uastar_engine;
 
 typedef struct {
     int32_t heaps;           /* k parallel binary heaps of the plain engine (0 -> 8192) */
-    int32_t block_threads;   /* CTA size of the plain engine's persistent kernel (0 -> 128) */
+    int32_t block_threads;   /* CTA size of the plain engine's persistent kernel (0 -> 256) */
     int32_t heap_capacity;   /* entries per heap (0 -> auto, grown on overflow) */
     int32_t hash_log2_slots; /* dedup table = 2^n slots of 32 B (0 -> auto from instance) */
     double max_load;         /* dedup table load limit in (0,1) (0 -> 0.9) */
     int64_t max_rounds;      /* GA* round limit per solve (0 -> 2^31) */
     double wait_timeout_s;   /* bound on any device-side barrier wait (0 -> 10 s) */
+    int32_t threads_per_heap; /* threads that share one heap's successors (0 -> 4 grid, 2 puzzle) */
+    int32_t heap_top_levels;  /* heap levels kept in shared memory (0 -> as many as fit, -1 -> none) */
 } uastar_config;
 
 /* Replaces GPUPathwaySolver/GPUPuzzleSolver construction + initialize()'s
@@ -181,10 +183,13 @@ typedef struct {
     int32_t attempts;         /* 1 + retries with a larger partition */
     int32_t reserved;
     double latency_ms;        /* serving: completion - arrival; batch: completion - launch */
+    double device_ms;         /* device time of the last attempt's search (CTA team) */
+    double start_ms;          /* batch: device start of the last attempt, from its wave's first start */
 } uastar_instance_result;
 
 typedef struct {
-    int32_t threads_per_instance; /* CTA size: heaps per instance (0 -> autotuned) */
+    int32_t threads_per_instance; /* CTA size per instance (0 -> 256) */
+    int32_t threads_per_heap;     /* heaps per instance = threads_per_instance / this (0 -> 1) */
     int32_t heap_capacity;        /* entries per heap (0 -> autotuned) */
     double load_factor;           /* target dedup-partition load (0 -> autotuned) */
     int32_t ctas;                 /* persistent CTAs (0 -> all SMs x occupancy) */
@@ -197,6 +202,7 @@ typedef struct {
     int64_t expanded;
     int64_t generated;
     int32_t waves;            /* launches (1 + retry waves) */
+    int32_t escalated;        /* instances re-solved by the plain engine */
     int32_t ctas;
     int32_t threads_per_instance;
     int32_t heap_capacity;
@@ -207,8 +213,10 @@ typedef struct {
 /* Solve `count` instances of mixed kinds in one persistent launch; each CTA
  * takes instances from a device work queue and runs GA* on it with its own
  * heap slice and dedup partition.  Instances whose partition or heaps
- * overflow are re-run in a later wave with 4x the space.  No counterpart in
- * the reference (spec extension of GPUPathwaySolver/GPUPuzzleSolver). */
+ * overflow are re-run in a second wave with 8x the partition (4x the heaps);
+ * those that overflow again are escalated to the plain engine.  No
+ * counterpart in the reference (spec extension of
+ * GPUPathwaySolver/GPUPuzzleSolver). */
 int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int32_t count,
                            const uastar_batch_config *cfg, uastar_instance_result *results,
                            uastar_batch_stats *stats);
@@ -222,6 +230,7 @@ typedef struct {
     double hbm_budget_gb;     /* admission budget for heaps + dedup partitions (default 120) */
     int32_t slots;            /* max concurrently resident requests (0 -> all CTAs) */
     int32_t threads_per_instance;
+    int32_t threads_per_heap;
     int32_t heap_capacity;
     int32_t rounds_per_quantum; /* GA* rounds per persistent-kernel launch (0 -> 256) */
     double load_factor;

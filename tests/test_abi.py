@@ -34,12 +34,12 @@ def test_bindings_cover_header():
 
 def test_struct_sizes_match_c_layout():
     # sizes computed from the header's field lists (natural alignment, x86-64 / aarch64)
-    assert C.sizeof(L.Config) == 40
+    assert C.sizeof(L.Config) == 48
     assert C.sizeof(L.GridResult) == 104
     assert C.sizeof(L.PuzzleResult) == 64
     assert C.sizeof(L.Instance) == 64
-    assert C.sizeof(L.InstanceResult) == 72
-    assert C.sizeof(L.ServeCompletion) == 80
+    assert C.sizeof(L.InstanceResult) == 88
+    assert C.sizeof(L.ServeCompletion) == 96
 
 
 def test_status_codes_match_header():

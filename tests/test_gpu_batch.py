@@ -67,7 +67,7 @@ def test_batch_overflow_retry_preserves_results(beng):
     specs = [WL.PuzzleSpec(4, 60, 77), WL.screened_grid(300, 300, 0.2, 3, exact=True)]
     insts = [s.instance(est_nodes=64) for s in specs]
     res, stats = beng.batch_solve(insts)
-    assert stats["waves"] >= 2
+    assert stats["waves"] >= 2 or stats["escalated"] >= 1
     p = beng.puzzle_solve(4, insts[0].tiles)
     assert res[0]["status"] == L.OK and res[0]["steps"] == p.steps and res[0]["attempts"] >= 2
     ex = O.grid_astar_exact(insts[1].words, 300, 300, (0, 0), (299, 299))

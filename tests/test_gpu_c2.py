@@ -19,7 +19,7 @@ def test_grid_20000():
     sp = WL.GRID_20000
     assert (c["H"], c["seed"]) == (sp.H, sp.seed)
     w = sp.words()
-    with Engine(0, heaps=8192, block_threads=128, hash_log2_slots=28) as eng:
+    with Engine(0, heaps=8192, block_threads=256, threads_per_heap=4, hash_log2_slots=28) as eng:
         r = eng.grid_solve(w, sp.H, sp.W, sp.start, sp.goal)
         path = eng.grid_path()
     assert r.ok

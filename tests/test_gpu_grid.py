@@ -38,9 +38,10 @@ def check_against(r, path, words, c):
     assert len(path) == r.path_len
 
 
-@pytest.mark.parametrize("heaps,block", [(8192, 128), (1024, 64), (32, 32)])
-def test_golden_small_grids(heaps, block):
-    with Engine(0, heaps=heaps, block_threads=block) as eng:
+@pytest.mark.parametrize("heaps,block,tph,levels", [(8192, 256, 4, 0), (8192, 128, 1, -1), (1024, 64, 2, 3),
+                                                    (32, 32, 1, 2), (64, 512, 8, 0)])
+def test_golden_small_grids(heaps, block, tph, levels):
+    with Engine(0, heaps=heaps, block_threads=block, threads_per_heap=tph, heap_top_levels=levels) as eng:
         for c in golden("grid_small.json"):
             w = case_words(c)
             r = eng.grid_solve(w, c["H"], c["W"], tuple(c["start"]), tuple(c["goal"]))
@@ -116,7 +117,7 @@ def test_auto_table_grows_on_overflow():
 
 def test_small_fixed_heaps_report_overflow():
     sp = WL.screened_grid(400, 400, 0.1, 1, exact=True)
-    with Engine(0, heaps=32, block_threads=32, heap_capacity=3) as eng:
+    with Engine(0, heaps=32, block_threads=32, threads_per_heap=1, heap_capacity=3, heap_top_levels=-1) as eng:
         r = eng.grid_solve(sp.words(), 400, 400, sp.start, sp.goal)
         assert r.status == L.HEAP_OVERFLOW
 

@@ -27,7 +27,7 @@ KIND_GRID, KIND_PUZZLE = 1, 2
 class Config(C.Structure):
     _fields_ = [("heaps", C.c_int32), ("block_threads", C.c_int32), ("heap_capacity", C.c_int32),
                 ("hash_log2_slots", C.c_int32), ("max_load", C.c_double), ("max_rounds", C.c_int64),
-                ("wait_timeout_s", C.c_double)]
+                ("wait_timeout_s", C.c_double), ("threads_per_heap", C.c_int32), ("heap_top_levels", C.c_int32)]
 
 
 class GridResult(C.Structure):
@@ -54,24 +54,27 @@ class InstanceResult(C.Structure):
     _fields_ = [("status", C.c_int32), ("steps", C.c_int32), ("straight", C.c_int64),
                 ("diagonal", C.c_int64), ("cost", C.c_float), ("pad", C.c_float),
                 ("expanded", C.c_int64), ("generated", C.c_int64), ("rounds", C.c_int64),
-                ("attempts", C.c_int32), ("reserved", C.c_int32), ("latency_ms", C.c_double)]
+                ("attempts", C.c_int32), ("reserved", C.c_int32), ("latency_ms", C.c_double),
+                ("device_ms", C.c_double), ("start_ms", C.c_double)]
 
 
 class BatchConfig(C.Structure):
-    _fields_ = [("threads_per_instance", C.c_int32), ("heap_capacity", C.c_int32),
-                ("load_factor", C.c_double), ("ctas", C.c_int32), ("use_graph", C.c_int32)]
+    _fields_ = [("threads_per_instance", C.c_int32), ("threads_per_heap", C.c_int32),
+                ("heap_capacity", C.c_int32), ("load_factor", C.c_double), ("ctas", C.c_int32),
+                ("use_graph", C.c_int32)]
 
 
 class BatchStats(C.Structure):
     _fields_ = [("wall_ms", C.c_double), ("kernel_ms", C.c_double), ("expanded", C.c_int64),
-                ("generated", C.c_int64), ("waves", C.c_int32), ("ctas", C.c_int32),
-                ("threads_per_instance", C.c_int32), ("heap_capacity", C.c_int32),
+                ("generated", C.c_int64), ("waves", C.c_int32), ("escalated", C.c_int32),
+                ("ctas", C.c_int32), ("threads_per_instance", C.c_int32), ("heap_capacity", C.c_int32),
                 ("load_factor", C.c_double), ("partition_bytes", C.c_int64)]
 
 
 class ServeConfig(C.Structure):
     _fields_ = [("hbm_budget_gb", C.c_double), ("slots", C.c_int32), ("threads_per_instance", C.c_int32),
-                ("heap_capacity", C.c_int32), ("rounds_per_quantum", C.c_int32), ("load_factor", C.c_double)]
+                ("threads_per_heap", C.c_int32), ("heap_capacity", C.c_int32), ("rounds_per_quantum", C.c_int32),
+                ("load_factor", C.c_double)]
 
 
 class ServeCompletion(C.Structure):

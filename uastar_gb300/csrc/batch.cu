@@ -42,11 +42,15 @@ struct InstDesc {
     uint32_t log2_slots;
     uint32_t fresh;       // serving: state not yet initialised
     uint64_t max_rounds;
+    uint64_t heap_off16;  // serving: first 16-byte entry of this request's heap slice
+    uint32_t heap_stride16;  // serving: entries per heap of that slice
+    uint32_t pad;
 };
 
 struct InstOut {
     uint32_t status, goal_slot;
     unsigned long long goal_best, rounds, expanded, generated, pushed, inserted;
+    unsigned long long t_start, t_end;  // device globaltimer around this call's work (ns)
 };
 
 struct BatchArgs {
@@ -57,10 +61,13 @@ struct BatchArgs {
     const uint8_t *pdb3;
     const uint8_t *pdb4;
     Slot *tab;
-    uint8_t *heaps;        // per CTA: blockDim heaps x stride16 x 16 bytes
+    uint8_t *heaps;        // per CTA: H heaps x stride16 x 16 bytes
     uint32_t stride16;     // heap stride in 16-byte entries (puzzles use 2x as 8-byte entries)
-    uint32_t *hsize;       // per CTA: blockDim
-    Cand *cand;            // per CTA: blockDim * 8
+    uint32_t *hsize;       // per CTA: H
+    Cand *cand;            // per CTA: H * 8
+    uint32_t H;            // heaps per instance (CTA)
+    uint32_t topn_grid;    // heap entries kept in shared memory (grid / puzzle entry sizes)
+    uint32_t topn_puzzle;
     InstOut *outs;
     TeamState *states;     // serving: per slot persisted team state
     double max_load;
@@ -84,7 +91,8 @@ __device__ void init_state(TeamState *st) {
 
 // Runs one instance on this CTA for up to `budget` rounds.
 __device__ uint32_t run_instance(const BatchArgs &a, const InstDesc &d, TeamState *st, uint8_t *heaps,
-                                 uint32_t *hs, Cand *cand, uint64_t budget) {
+                                 uint32_t stride16, uint32_t *hs, Cand *cand, unsigned char *smem,
+                                 uint64_t budget) {
     BlockTeam team{st};
     Slot *tab = a.tab + d.tab_off;
     const uint64_t slots = 1ull << d.log2_slots;
@@ -98,8 +106,8 @@ __device__ uint32_t run_instance(const BatchArgs &a, const InstDesc &d, TeamStat
         prob.ex = d.ex;
         prob.ey = d.ey;
         SearchMem<GridEntry> m{tab, slots - 1, (uint64_t)(slots * a.max_load), 4096u,
-                               reinterpret_cast<GridEntry *>(heaps), a.stride16, hs, cand, d.max_rounds};
-        return ga_search(prob, team, m, budget);
+                               reinterpret_cast<GridEntry *>(heaps), stride16, hs, cand, d.max_rounds};
+        return ga_search(prob, team, m, a.H, a.topn_grid, smem, budget);
     }
     if (d.n == 4) {
         PuzzleProblem<4> prob;
@@ -107,26 +115,30 @@ __device__ uint32_t run_instance(const BatchArgs &a, const InstDesc &d, TeamStat
         prob.start = d.start_key;
         prob.goal = PuzzleProblem<4>::goal_key();
         SearchMem<PuzzleEntry> m{tab, slots - 1, (uint64_t)(slots * a.max_load), 4096u,
-                                 reinterpret_cast<PuzzleEntry *>(heaps), a.stride16 * 2, hs, cand,
+                                 reinterpret_cast<PuzzleEntry *>(heaps), stride16 * 2, hs, cand,
                                  d.max_rounds};
-        return ga_search(prob, team, m, budget);
+        return ga_search(prob, team, m, a.H, a.topn_puzzle, smem, budget);
     }
     PuzzleProblem<3> prob;
     prob.pdb = a.pdb3;
     prob.start = d.start_key;
     prob.goal = PuzzleProblem<3>::goal_key();
     SearchMem<PuzzleEntry> m{tab, slots - 1, (uint64_t)(slots * a.max_load), 4096u,
-                             reinterpret_cast<PuzzleEntry *>(heaps), a.stride16 * 2, hs, cand, d.max_rounds};
-    return ga_search(prob, team, m, budget);
+                             reinterpret_cast<PuzzleEntry *>(heaps), stride16 * 2, hs, cand, d.max_rounds};
+    return ga_search(prob, team, m, a.H, a.topn_puzzle, smem, budget);
 }
 
 __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
     __shared__ TeamState st;
     __shared__ uint32_t s_next;
-    const uint32_t T = blockDim.x;
-    uint8_t *heaps = a.heaps + (size_t)blockIdx.x * T * a.stride16 * 16;
-    uint32_t *hs = a.hsize + (size_t)blockIdx.x * T;
-    Cand *cand = a.cand + (size_t)blockIdx.x * T * 8;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t H = a.H;
+    // batch: each CTA owns a heap slice reused by the instances it takes;
+    // serving: each request owns a slice named by its descriptor
+    uint8_t *heaps = a.heaps + (size_t)blockIdx.x * H * a.stride16 * 16;
+    uint32_t stride16 = a.stride16;
+    uint32_t *hs = a.hsize + (size_t)blockIdx.x * H;
+    Cand *cand = a.cand + (size_t)blockIdx.x * H * 8;
     for (uint32_t iter = 0;; ++iter) {
         if (a.serving) {
             if (iter > 0 || blockIdx.x >= a.count) break;
@@ -139,15 +151,20 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
         if (i >= a.count) break;
         const InstDesc d = a.descs[i];
         if (a.serving && d.kind == 0) break;  // empty serving slot
+        const unsigned long long t_start = globaltimer_ns();
+        if (a.serving) {
+            heaps = a.heaps + d.heap_off16 * 16;
+            stride16 = d.heap_stride16;
+        }
         if (!a.serving || d.fresh) {
             clear_partition(a.tab + d.tab_off, 1ull << d.log2_slots);
-            for (uint32_t j = threadIdx.x; j < T; j += T) hs[j] = 0;
+            for (uint32_t j = threadIdx.x; j < H; j += blockDim.x) hs[j] = 0;
             if (threadIdx.x == 0) init_state(&st);
         } else if (threadIdx.x == 0) {
             st = a.states[i];
         }
         __syncthreads();
-        run_instance(a, d, &st, heaps, hs, cand, a.budget);
+        run_instance(a, d, &st, heaps, stride16, hs, cand, smem, a.budget);
         __syncthreads();
         if (threadIdx.x == 0) {
             InstOut o;
@@ -159,6 +176,8 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
             o.generated = st.generated;
             o.pushed = st.pushed;
             o.inserted = st.inserted;
+            o.t_start = t_start;
+            o.t_end = globaltimer_ns();
             // a phase-2 error of the last round of a quantum is still in error2
             if (o.status == ST_RUNNING && (st.error || st.error2[0] || st.error2[1]))
                 o.status = st.error ? st.error : (st.error2[0] ? st.error2[0] : st.error2[1]);
@@ -263,21 +282,53 @@ int32_t check_instance(const uastar_instance &in) {
 
 struct BatchGeometry {
     int T, ctas;
+    uint32_t H, topn_grid, topn_puzzle;
     uint32_t stride16;
+    size_t smem;
     double load;
 };
 
-int32_t resolve_geometry(uastar_engine *eng, const uastar_batch_config *cfg, BatchGeometry *g) {
-    g->T = cfg && cfg->threads_per_instance > 0 ? cfg->threads_per_instance : 256;
+// Largest 2^L - 1 heap-top entries per heap whose shared memory fits `budget`.
+template <class P> uint32_t fit_top(uint32_t H, size_t budget) {
+    uint32_t best = 0;
+    for (int L = 1; L <= 10; ++L) {
+        const uint32_t topn = (1u << L) - 1;
+        if (SearchSmem<P>::bytes(H, topn) > budget) break;
+        best = topn;
+    }
+    return best;
+}
+
+// CTA size, heaps per CTA, shared heap tops sized for two CTAs per SM.
+int32_t resolve_block_geometry(uastar_engine *eng, int threads, int tph, BatchGeometry *g) {
+    g->T = threads > 0 ? threads : 256;
     g->T = std::max(32, std::min(512, (g->T + 31) / 32 * 32));
+    tph = std::max(1, std::min(tph > 0 ? tph : 1, g->T));
+    g->H = (uint32_t)std::max(1, g->T / tph);
+    int smem_sm = 0;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, eng->device);
+    const size_t per_cta = (size_t)std::max(16 * 1024, smem_sm / 2 - 4 * 1024);
+    g->topn_grid = fit_top<GridProblem>(g->H, per_cta);
+    g->topn_puzzle = fit_top<PuzzleProblem<4>>(g->H, per_cta);
+    g->smem = std::max(SearchSmem<GridProblem>::bytes(g->H, g->topn_grid),
+                       SearchSmem<PuzzleProblem<4>>::bytes(g->H, g->topn_puzzle));
+    cudaError_t e = cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g->smem);
+    if (e != cudaSuccess) return fail_cuda(eng, e, "smem attribute");
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch, g->T, g->smem);
+    if (e != cudaSuccess) return fail_cuda(eng, e, "occupancy");
+    g->ctas = eng->sms * std::max(1, occ);
+    return UASTAR_OK;
+}
+
+int32_t resolve_geometry(uastar_engine *eng, const uastar_batch_config *cfg, BatchGeometry *g) {
+    int32_t rc = resolve_block_geometry(eng, cfg ? cfg->threads_per_instance : 0, cfg ? cfg->threads_per_heap : 0, g);
+    if (rc) return rc;
     const uint32_t cap = cfg && cfg->heap_capacity > 0 ? (uint32_t)cfg->heap_capacity : 2048;
     g->stride16 = (uint32_t)next_pow2_u64(cap + 1);
+    g->stride16 = std::max<uint32_t>(g->stride16, (uint32_t)next_pow2_u64(std::max(g->topn_grid, g->topn_puzzle / 2) + 2));
     g->load = cfg && cfg->load_factor > 0 && cfg->load_factor < 1 ? cfg->load_factor : 0.5;
-    int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch, g->T, 0);
-    if (e != cudaSuccess) return fail_cuda(eng, e, "occupancy");
-    occ = std::max(1, occ);
-    g->ctas = cfg && cfg->ctas > 0 ? cfg->ctas : eng->sms * occ;
+    if (cfg && cfg->ctas > 0) g->ctas = std::min(g->ctas, cfg->ctas);
     return UASTAR_OK;
 }
 
@@ -327,11 +378,11 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
     }
     // device buffers
     const size_t tab_b = tab_slots * sizeof(Slot);
-    const size_t heap_b = (size_t)g.ctas * g.T * g.stride16 * 16;
+    const size_t heap_b = (size_t)g.ctas * g.H * g.stride16 * 16;
     if ((e = eng->b_tab.ensure(tab_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc partitions");
     if ((e = eng->b_heaps.ensure(heap_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc heap slices");
-    if ((e = eng->b_hsize.ensure((size_t)g.ctas * g.T * 4)) != cudaSuccess) return fail_cuda(eng, e, "alloc");
-    if ((e = eng->b_cand.ensure((size_t)g.ctas * g.T * 8 * sizeof(Cand))) != cudaSuccess)
+    if ((e = eng->b_hsize.ensure((size_t)g.ctas * g.H * 4)) != cudaSuccess) return fail_cuda(eng, e, "alloc");
+    if ((e = eng->b_cand.ensure((size_t)g.ctas * g.H * 8 * sizeof(Cand))) != cudaSuccess)
         return fail_cuda(eng, e, "alloc");
     if ((e = eng->b_desc.ensure(cnt * sizeof(InstDesc))) != cudaSuccess) return fail_cuda(eng, e, "alloc");
     if ((e = eng->b_out.ensure(cnt * sizeof(InstOut))) != cudaSuccess) return fail_cuda(eng, e, "alloc");
@@ -369,6 +420,9 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
     a.max_load = 0.9;
     a.budget = ~0ull;
     a.serving = 0;
+    a.H = g.H;
+    a.topn_grid = g.topn_grid;
+    a.topn_puzzle = g.topn_puzzle;
     const int ctas = std::min(g.ctas, cnt);
 
     cudaEvent_t k0, k1;
@@ -378,7 +432,7 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
     cudaGraphExec_t exec = nullptr;
     auto enqueue = [&]() {
         cudaMemsetAsync(eng->b_queue.p, 0, 4, eng->stream);
-        k_batch<<<ctas, g.T, 0, eng->stream>>>(a);
+        k_batch<<<ctas, g.T, g.smem, eng->stream>>>(a);
     };
     cudaEventRecord(k0, eng->stream);
     if (use_graph) {
@@ -449,6 +503,8 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
     }
     std::vector<int> walk_of(cnt, -1);
     for (size_t w = 0; w < which.size(); ++w) walk_of[which[w]] = (int)w;
+    unsigned long long t_first = ~0ull;
+    for (int p = 0; p < cnt; ++p) t_first = std::min(t_first, outs[p].t_start);
 
     for (int j = 0; j < cnt; ++j) {
         const int p = slot_of[j];
@@ -456,6 +512,8 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
         const uastar_instance &in = insts[idx[j]];
         uastar_instance_result &r = results[idx[j]];
         r.attempts += 1;
+        r.device_ms = (double)(o.t_end - o.t_start) * 1e-6;
+        r.start_ms = (double)(o.t_start - t_first) * 1e-6;
         r.status = (int32_t)o.status;
         r.expanded += (int64_t)o.expanded;
         r.generated += (int64_t)o.generated;
@@ -557,7 +615,10 @@ int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int
     std::vector<int> mult(count, 1);
     BatchGeometry gw = g;
     const bool use_graph = !cfg || cfg->use_graph != 0 || cfg->threads_per_instance == 0;
-    for (int wave = 0; wave < 5 && !todo.empty(); ++wave) {
+    // Waves of CTA teams; an instance that overflowed twice is a large one and
+    // is escalated to the plain engine (the whole GPU as its team, tables
+    // grown in place of a third wave).
+    for (int wave = 0; wave < 2 && !todo.empty(); ++wave) {
         std::vector<int> retry, m(todo.size());
         for (size_t j = 0; j < todo.size(); ++j) m[j] = mult[todo[j]];
         rc = run_wave(eng, insts, todo, gw, m, use_graph, results, stats, &retry);
@@ -569,6 +630,42 @@ int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int
         // a retry wave runs fewer instances: fewer CTAs keep the heap slices small
         gw.ctas = std::min<int>(g.ctas, std::max<int>(1, (int)retry.size()));
         todo.swap(retry);
+    }
+    // the partitions of a large batch can hold a large share of HBM: return them
+    eng->b_tab.release();
+    eng->b_bitmaps.release();
+    for (int i : todo) {
+        const uastar_instance &in = insts[i];
+        uastar_instance_result &r = results[i];
+        r.attempts += 1;
+        if (in.kind == UASTAR_KIND_GRID) {
+            uastar_grid_result gr;
+            rc = uastar_grid_solve(eng, in.words, in.H, in.W, in.sx, in.sy, in.ex, in.ey, &gr);
+            r.status = gr.status;
+            r.straight = gr.straight;
+            r.diagonal = gr.diagonal;
+            r.cost = gr.cost;
+            r.expanded += gr.expanded;
+            r.generated += gr.generated;
+            r.rounds += gr.rounds;
+            if (stats) {
+                stats->expanded += gr.expanded;
+                stats->generated += gr.generated;
+            }
+        } else {
+            uastar_puzzle_result pr;
+            rc = uastar_puzzle_solve(eng, in.n, in.tiles, &pr);
+            r.status = pr.status;
+            r.steps = pr.steps;
+            r.expanded += pr.expanded;
+            r.generated += pr.generated;
+            r.rounds += pr.rounds;
+            if (stats) {
+                stats->expanded += pr.expanded;
+                stats->generated += pr.generated;
+            }
+        }
+        if (stats) stats->escalated += 1;
     }
     if (stats) {
         stats->wall_ms = now_ms() - t0;
@@ -585,16 +682,19 @@ int32_t uastar_autotune(uastar_engine *eng, const uastar_instance *sample, int32
                         uastar_batch_config *best) {
     if (!eng || !sample || count <= 0 || !best) return UASTAR_BAD_INPUT;
     const int Ts[] = {128, 256, 512};
-    const int caps[] = {1024, 4096};
+    const int tphs[] = {1, 2};
+    const int caps[] = {2048};
     const double loads[] = {0.35, 0.6};
     std::vector<uastar_instance_result> res(count);
     double best_ms = 1e300;
     uastar_batch_config pick{};
     for (int T : Ts)
+        for (int tph : tphs)
         for (int cap : caps)
             for (double ld : loads) {
                 uastar_batch_config c{};
                 c.threads_per_instance = T;
+                c.threads_per_heap = tph;
                 c.heap_capacity = cap;
                 c.load_factor = ld;
                 c.use_graph = 1;
@@ -675,7 +775,8 @@ struct ServeReq {
     uastar_instance inst{};
     std::vector<uint64_t> words;  // owned copy of the grid bitmap
     double arrival_s = 0;
-    uint64_t mult = 1;
+    uint64_t mult = 1;            // dedup partition growth after HASH_FULL
+    uint32_t heap_mult = 1;       // heap slice growth after HEAP_OVERFLOW
     int attempts = 0;
     uastar_instance_result acc{};
 };
@@ -683,13 +784,14 @@ struct ServeReq {
 struct ServeSlotState {
     bool busy = false;
     ServeReq req;
-    uint64_t tab_off = 0, tab_n = 0, bm_off = 0, bm_n = 0;
+    uint64_t tab_off = 0, tab_n = 0, bm_off = 0, bm_n = 0, heap_off = 0, heap_n = 0;
 };
 
 struct ServeState {
     uastar_engine *eng = nullptr;
     uastar_serve_config cfg{};
     int T = 256, S = 0;
+    BatchGeometry geo{};
     uint32_t stride16 = 2048;
     uint64_t heap_bytes = 0;
     std::thread th;
@@ -705,7 +807,7 @@ struct ServeState {
     int32_t loop_error = UASTAR_OK;
     // device state
     DevBuf tab, bitmaps, heaps, hsize, cand, descs, outs, states, walk;
-    RangeAlloc tab_alloc, bm_alloc;
+    RangeAlloc tab_alloc, bm_alloc, heap_alloc;  // units: slots, 8-byte words, 16-byte heap entries
     cudaStream_t stream = nullptr;
     cudaEvent_t q0 = nullptr, q1 = nullptr;
 };
@@ -769,6 +871,7 @@ static void serve_loop(ServeState *S) {
                         serve_complete(S, slots[s].req, UASTAR_CANCELLED);
                         S->tab_alloc.release(slots[s].tab_off, slots[s].tab_n);
                         if (slots[s].bm_n) S->bm_alloc.release(slots[s].bm_off, slots[s].bm_n);
+                        S->heap_alloc.release(slots[s].heap_off, slots[s].heap_n);
                         slots[s] = ServeSlotState();
                         descs[s].kind = 0;
                     }
@@ -786,14 +889,21 @@ static void serve_loop(ServeState *S) {
             if (free_slot >= S->S) break;
             const uint64_t tn = serve_partition_slots(S, r);
             const uint64_t bn = r.inst.kind == UASTAR_KIND_GRID ? r.words.size() + 2 : 0;
-            if (tn > S->tab_alloc.capacity() || bn > S->bm_alloc.capacity()) {
+            const uint32_t hstride = S->stride16 * r.heap_mult;
+            const uint64_t hn = (uint64_t)S->geo.H * hstride;
+            if (tn > S->tab_alloc.capacity() || bn > S->bm_alloc.capacity() || hn > S->heap_alloc.capacity()) {
                 serve_complete(S, r, UASTAR_REJECTED);  // can never fit the budget
                 continue;
             }
-            uint64_t toff = 0, boff = 0;
+            uint64_t toff = 0, boff = 0, hoff = 0;
             if (!S->tab_alloc.alloc(tn, 1, &toff)) break;  // wait for memory to free up
             if (bn && !S->bm_alloc.alloc(bn, 2, &boff)) {
                 S->tab_alloc.release(toff, tn);
+                break;
+            }
+            if (!S->heap_alloc.alloc(hn, 2, &hoff)) {
+                S->tab_alloc.release(toff, tn);
+                if (bn) S->bm_alloc.release(boff, bn);
                 break;
             }
             ServeSlotState &sl = slots[free_slot];
@@ -802,6 +912,8 @@ static void serve_loop(ServeState *S) {
             sl.tab_n = tn;
             sl.bm_off = boff;
             sl.bm_n = bn;
+            sl.heap_off = hoff;
+            sl.heap_n = hn;
             sl.req = std::move(r);
             sl.req.attempts += 1;
             InstDesc d;
@@ -812,6 +924,8 @@ static void serve_loop(ServeState *S) {
             d.tab_off = toff;
             d.log2_slots = (uint32_t)log2_u64(tn);
             d.fresh = 1;
+            d.heap_off16 = hoff;
+            d.heap_stride16 = hstride;
             if (d.kind == UASTAR_KIND_GRID) {
                 d.H = sl.req.inst.H;
                 d.W = sl.req.inst.W;
@@ -834,7 +948,8 @@ static void serve_loop(ServeState *S) {
         S->stats.peak_resident = std::max(S->stats.peak_resident, resident);
         S->stats.peak_budget_gb =
             std::max(S->stats.peak_budget_gb, ((double)S->tab_alloc.used() * sizeof(Slot) +
-                                               (double)S->bm_alloc.used() * 8 + (double)S->heap_bytes) /
+                                               (double)S->bm_alloc.used() * 8 +
+                                               (double)S->heap_alloc.used() * 16) /
                                                   1e9);
         if (resident == 0) {
             std::unique_lock<std::mutex> lk(S->mu);
@@ -866,10 +981,13 @@ static void serve_loop(ServeState *S) {
         a.outs = S->outs.as<InstOut>();
         a.states = S->states.as<TeamState>();
         a.max_load = 0.9;
+        a.H = S->geo.H;
+        a.topn_grid = S->geo.topn_grid;
+        a.topn_puzzle = S->geo.topn_puzzle;
         a.budget = (uint64_t)(S->cfg.rounds_per_quantum > 0 ? S->cfg.rounds_per_quantum : 256);
         a.serving = 1;
         cudaEventRecord(S->q0, S->stream);
-        k_batch<<<S->S, S->T, 0, S->stream>>>(a);
+        k_batch<<<S->S, S->T, S->geo.smem, S->stream>>>(a);
         eng->launches++;
         cudaEventRecord(S->q1, S->stream);
         e = cudaGetLastError();
@@ -935,15 +1053,19 @@ static void serve_loop(ServeState *S) {
             if (!sl.busy || outs[s].status == ST_RUNNING) continue;
             const InstOut &o = outs[s];
             ServeReq &r = sl.req;
+            r.acc.device_ms = (double)(o.t_end - o.t_start) * 1e-6;
             r.acc.expanded += (int64_t)o.expanded;
             r.acc.generated += (int64_t)o.generated;
             r.acc.rounds += (int64_t)o.rounds;
             int32_t status = (int32_t)o.status;
             S->tab_alloc.release(sl.tab_off, sl.tab_n);
             if (sl.bm_n) S->bm_alloc.release(sl.bm_off, sl.bm_n);
+            S->heap_alloc.release(sl.heap_off, sl.heap_n);
             descs[s].kind = 0;
-            if ((status == ST_HASH_FULL || status == ST_HEAP_OVERFLOW) && r.attempts < 5) {
-                r.mult *= 8;  // re-queue with a larger partition, ahead of later arrivals
+            if ((status == ST_HASH_FULL || status == ST_HEAP_OVERFLOW) && r.attempts < 10) {
+                // re-queue with 4x the space, ahead of later arrivals
+                if (status == ST_HASH_FULL) r.mult *= 4;
+                else r.heap_mult *= 4;
                 pending.insert(pending.begin(), std::move(r));
                 sl = ServeSlotState();
                 continue;
@@ -1022,34 +1144,39 @@ int32_t uastar_serve_start(uastar_engine *eng, const uastar_serve_config *cfg) {
     S->eng = eng;
     if (cfg) S->cfg = *cfg;
     if (!(S->cfg.hbm_budget_gb > 0)) S->cfg.hbm_budget_gb = 120.0;
-    S->T = S->cfg.threads_per_instance > 0 ? std::max(32, std::min(512, (S->cfg.threads_per_instance + 31) / 32 * 32))
-                                           : 256;
-    S->stride16 = (uint32_t)next_pow2_u64((uint64_t)(S->cfg.heap_capacity > 0 ? S->cfg.heap_capacity : 2048) + 1);
-    int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch, S->T, 0);
-    if (e != cudaSuccess) {
+    int32_t grc = resolve_block_geometry(eng, S->cfg.threads_per_instance, S->cfg.threads_per_heap, &S->geo);
+    if (grc) {
         delete S;
-        return fail_cuda(eng, e, "occupancy");
+        return grc;
     }
-    const int max_slots = eng->sms * std::max(1, occ);
+    S->T = S->geo.T;
+    S->stride16 = (uint32_t)next_pow2_u64((uint64_t)(S->cfg.heap_capacity > 0 ? S->cfg.heap_capacity : 2048) + 1);
+    S->stride16 = std::max<uint32_t>(
+        S->stride16, (uint32_t)next_pow2_u64(std::max(S->geo.topn_grid, S->geo.topn_puzzle / 2) + 2));
+    const int max_slots = S->geo.ctas;
+    cudaError_t e = cudaSuccess;
     S->S = S->cfg.slots > 0 ? std::min(S->cfg.slots, max_slots) : max_slots;
+    // The budget is split into three arenas that requests draw from:
+    // heap slices (20 %), grid bitmaps (5 %) and dedup partitions (75 %).
     const double budget_b = S->cfg.hbm_budget_gb * 1e9;
-    S->heap_bytes = (uint64_t)S->S * S->T * S->stride16 * 16;
+    const uint64_t heap_entries = (uint64_t)(budget_b * 0.20 / 16);
     const uint64_t bm_words = (uint64_t)(budget_b * 0.05 / 8);
-    const double tab_b = budget_b - (double)S->heap_bytes - (double)bm_words * 8;
-    if (tab_b < (double)(1u << 20) * sizeof(Slot)) {
+    const double tab_b = budget_b * 0.75;
+    S->heap_bytes = heap_entries * 16;
+    if (tab_b < (double)(1u << 20) * sizeof(Slot) || heap_entries < (uint64_t)S->geo.H * S->stride16) {
         delete S;
-        eng->set_err("serving budget too small for the heap slices");
+        eng->set_err("serving budget too small");
         return UASTAR_BAD_INPUT;
     }
     const uint64_t tab_slots = (uint64_t)(tab_b / sizeof(Slot));
     S->tab_alloc.reset(tab_slots);
     S->bm_alloc.reset(bm_words);
+    S->heap_alloc.reset(heap_entries);
     if ((e = S->tab.ensure(tab_slots * sizeof(Slot))) != cudaSuccess ||
         (e = S->bitmaps.ensure(bm_words * 8 + 64)) != cudaSuccess ||
         (e = S->heaps.ensure(S->heap_bytes)) != cudaSuccess ||
-        (e = S->hsize.ensure((size_t)S->S * S->T * 4)) != cudaSuccess ||
-        (e = S->cand.ensure((size_t)S->S * S->T * 8 * sizeof(Cand))) != cudaSuccess ||
+        (e = S->hsize.ensure((size_t)S->S * S->geo.H * 4)) != cudaSuccess ||
+        (e = S->cand.ensure((size_t)S->S * S->geo.H * 8 * sizeof(Cand))) != cudaSuccess ||
         (e = S->descs.ensure((size_t)S->S * sizeof(InstDesc))) != cudaSuccess ||
         (e = S->outs.ensure((size_t)S->S * sizeof(InstOut))) != cudaSuccess ||
         (e = S->states.ensure((size_t)S->S * sizeof(TeamState))) != cudaSuccess ||

@@ -28,10 +28,12 @@ __global__ void k_fill_ff(uint4 *p, size_t n16) {
 }
 
 template <class P>
-__global__ void __launch_bounds__(256, 1) k_plain_search(P prob, SearchMem<typename P::Entry> m,
-                                                      TeamState *st, uint64_t timeout_ns) {
+__global__ void __launch_bounds__(512, 1) k_plain_search(P prob, SearchMem<typename P::Entry> m,
+                                                      TeamState *st, uint64_t timeout_ns, uint32_t H,
+                                                      uint32_t topn) {
+    extern __shared__ __align__(16) unsigned char smem[];
     GridTeam team{st, 0u, timeout_ns};
-    ga_search<P>(prob, team, m, ~0ull);
+    ga_search<P>(prob, team, m, H, topn, smem, ~0ull);
 }
 
 // Walk the prev chain from the goal slot (one thread: a pointer chase).
@@ -100,25 +102,52 @@ struct PlainOut {
 
 // Run one instance with the whole GPU as the team.  Grows the dedup table /
 // heaps and retries when they overflow and were auto-sized.
+// Shared-memory heap levels that fit: the largest L with H * 2^L entries
+// (plus the pop records) under `budget` bytes.
+template <class P> uint32_t fit_topn(uint32_t H, int levels, size_t budget) {
+    if (levels < 0) return 0;
+    uint32_t best = 0;
+    for (int L = 1; L <= 12; ++L) {
+        const uint32_t topn = (1u << L) - 1;
+        if (SearchSmem<P>::bytes(H, topn) > budget) break;
+        best = topn;
+        if (levels > 0 && L == levels) break;
+    }
+    return best;
+}
+
 template <class P>
 int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t stride_auto,
                   PlainOut *out) {
     using E = typename P::Entry;
     const uastar_config &c = eng->cfg;
     const uint32_t block = (uint32_t)c.block_threads;
-    const uint32_t nblocks = (uint32_t)((c.heaps + c.block_threads - 1) / c.block_threads);
-    const uint32_t k = nblocks * block;
+    const uint32_t tph = c.threads_per_heap > 0 ? (uint32_t)c.threads_per_heap : (P::kMoves >= 8 ? 4u : 2u);
+    const uint32_t H = std::max(1u, block / std::min(tph, block));
+    const uint32_t nblocks = (uint32_t)((c.heaps + H - 1) / H);
+    const uint32_t k = nblocks * H;
     int log2 = c.hash_log2_slots > 0 ? c.hash_log2_slots : log2_auto;
     uint32_t stride = c.heap_capacity > 0 ? next_pow2_u32((uint32_t)c.heap_capacity + 1) : stride_auto;
 
+    // shared heap tops: as many levels as fit while the whole team stays
+    // co-resident (ceil(nblocks / SMs) CTAs per SM)
+    int smem_optin = 0, smem_sm = 0;
+    cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, eng->device);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, eng->device);
+    const int per_sm = (int)((nblocks + eng->sms - 1) / eng->sms);
+    const size_t smem_budget = (size_t)std::max(8 * 1024, std::min(smem_optin, smem_sm / std::max(1, per_sm) - 2048));
+    const uint32_t topn = fit_topn<P>(H, c.heap_top_levels, smem_budget);
+    const size_t smem = SearchSmem<P>::bytes(H, topn);
+    cudaError_t e = cudaFuncSetAttribute(k_plain_search<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return fail_cuda(eng, e, "smem attribute");
     int max_active = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_active, k_plain_search<P>,
-                                                                  (int)block, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_active, k_plain_search<P>, (int)block, smem);
     if (e != cudaSuccess) return fail_cuda(eng, e, "occupancy");
     if ((uint64_t)max_active * eng->sms < nblocks) {
-        eng->set_err("heaps/block_threads exceed one co-resident wave of the GPU");
+        eng->set_err("heaps / (block_threads / threads_per_heap) exceed one co-resident wave of the GPU");
         return UASTAR_BAD_INPUT;
     }
+    if (stride <= topn + 1) stride = next_pow2_u32(topn + 2);
 
     for (int attempt = 0; attempt < 6; ++attempt) {
         const uint64_t slots = 1ull << log2;
@@ -153,10 +182,11 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
         TeamState *st = eng->team.as<TeamState>();
         uint64_t timeout_ns = (uint64_t)(c.wait_timeout_s * 1e9);
         P pr = prob;
-        void *args[] = {&pr, &m, &st, &timeout_ns};
+        uint32_t h_arg = H, topn_arg = topn;
+        void *args[] = {&pr, &m, &st, &timeout_ns, &h_arg, &topn_arg};
         cudaEventRecord(eng->ev0, eng->stream);
         e = cudaLaunchCooperativeKernel((const void *)k_plain_search<P>, dim3(nblocks), dim3(block),
-                                        args, 0, eng->stream);
+                                        args, smem, eng->stream);
         if (e != cudaSuccess) return fail_cuda(eng, e, "cooperative launch");
         eng->launches++;
         cudaEventRecord(eng->ev1, eng->stream);
@@ -367,8 +397,8 @@ uastar_engine *uastar_create(int32_t ordinal, const uastar_config *cfg) {
     if (cfg) eng->cfg = *cfg;
     uastar_config &c = eng->cfg;
     if (c.heaps <= 0) c.heaps = 8192;
-    if (c.block_threads <= 0) c.block_threads = 128;
-    c.block_threads = std::max(32, std::min(256, (c.block_threads + 31) / 32 * 32));
+    if (c.block_threads <= 0) c.block_threads = 256;
+    c.block_threads = std::max(32, std::min(512, (c.block_threads + 31) / 32 * 32));
     if (!(c.max_load > 0.0 && c.max_load < 1.0)) c.max_load = 0.9;
     if (c.max_rounds <= 0) c.max_rounds = 1ll << 31;
     if (!(c.wait_timeout_s > 0.0)) c.wait_timeout_s = 10.0;

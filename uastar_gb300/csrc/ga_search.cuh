@@ -2,25 +2,32 @@
 // that runs it (the whole cooperative grid for one large instance, or one
 // CTA per instance in the batched and serving engines).
 //
-// Each team thread owns one binary min-heap for popping.  A round is:
+// A team is C CTAs of T threads; each CTA owns H binary min-heaps (the first
+// H threads are their owners, T / H threads per heap), so the team has
+// k = C * H heaps.  A round is:
 //
-//   phase 1  every thread pops the minimum of its own heap; the team's
-//            minimum popped f is reduced (warp shuffles, one CAS per warp);
-//            stale entries (f no longer matching the node's g) are dropped;
-//            a goal pop lowers goal_best; every other pop is expanded.
-//            The warp then spreads all successors of its 32 pops evenly over
-//            its lanes; each lane finds-or-inserts its successor in the
-//            open-addressed dedup table (atomicCAS on the key) and lowers the
-//            slot's g with a CAS loop.  Only a strict improvement makes the
-//            successor a candidate, so among equal-g writers of one slot in a
-//            round exactly one candidate carries the final g.
+//   phase 1  each heap owner pops its heap's minimum; the round's minimum
+//            popped f is reduced (warp shuffles, one CAS per warp); stale
+//            entries (f no longer matching the node's g) are dropped; a goal
+//            pop lowers goal_best; every other pop is expanded.  The CTA then
+//            spreads the successors of its H pops over all T threads; each
+//            thread relaxes its successor in the open-addressed dedup table
+//            with one 16-byte CAS on (key, g): it either claims an empty slot
+//            with its g, or learns the slot's g and lowers it with a CAS loop.
+//            Only a strict improvement makes the successor a candidate, so
+//            among equal-g writers of one slot in a round exactly one
+//            candidate carries the final g.
 //   barrier  then a uniform decision: stop when goal_best <= the round's
 //            minimum popped f (the GA* optimality test of the reference,
 //            src/pathway/GPU-solver.cu:219-243), fail when nothing was popped.
-//   phase 2  candidates are pushed round-robin over all heaps; a candidate is
-//            the slot's winner iff the slot's g still equals its g, and only
-//            the winner writes prev/aux and pushes.
+//   phase 2  CTA c takes candidates c, c + C, c + 2C, ... of the round's n and
+//            deals them round-robin over its own heaps; a candidate is the
+//            slot's winner iff the slot's g still equals its g, and only the
+//            winner writes prev/aux and pushes.
 //   barrier
+//
+// Heaps are CTA-private, so the top levels of every heap live in shared
+// memory (a pop touches global memory only below them).
 //
 // This replaces the reference's per-round kExtractExpand -> host copy ->
 // MergesortPairs -> kAssign -> host copy -> kDeduplicate -> kHeapInsert
@@ -40,10 +47,10 @@ template <class E> struct SearchMem {
     uint64_t mask;          // slots - 1 (power of two)
     uint64_t max_inserted;  // load limit
     uint32_t max_probe;
-    E *heaps;               // team.size() heaps of `stride` entries; index 0 unused
+    E *heaps;               // k heaps of `stride` entries (index 0 unused), CTA c owns [c*H, (c+1)*H)
     uint32_t stride;
-    uint32_t *heap_size;
-    Cand *cand;             // >= team.size() * kMoves records
+    uint32_t *heap_size;    // k sizes
+    Cand *cand;             // >= k * kMoves records
     uint64_t max_rounds;    // absolute round limit (ITER_LIMIT)
 };
 
@@ -52,8 +59,8 @@ struct GridTeam {
     TeamState *st;  // global memory
     uint32_t epoch;
     uint64_t timeout_ns;
-    __device__ uint32_t rank() const { return blockIdx.x * blockDim.x + threadIdx.x; }
-    __device__ uint32_t size() const { return gridDim.x * blockDim.x; }
+    __device__ uint32_t cta() const { return blockIdx.x; }
+    __device__ uint32_t ctas() const { return gridDim.x; }
     __device__ void sync() { grid_barrier(&st->barrier, gridDim.x, epoch, &st->error, timeout_ns); }
     __device__ uint64_t rd64(const unsigned long long *p) const { return ldcg_u64(p); }
     __device__ uint32_t rd32(const uint32_t *p) const { return ldcg_u32(p); }
@@ -61,8 +68,8 @@ struct GridTeam {
 
 struct BlockTeam {
     TeamState *st;  // shared memory
-    __device__ uint32_t rank() const { return threadIdx.x; }
-    __device__ uint32_t size() const { return blockDim.x; }
+    __device__ uint32_t cta() const { return 0; }
+    __device__ uint32_t ctas() const { return 1; }
     __device__ void sync() { __syncthreads(); }
     __device__ uint64_t rd64(const unsigned long long *p) const {
         return *reinterpret_cast<const volatile unsigned long long *>(p);
@@ -73,50 +80,63 @@ struct BlockTeam {
 };
 
 // ------------------------------------------------------------------ heaps ---
-// 1-indexed binary heap in global memory; the two children 2i, 2i+1 of a
-// node are adjacent (one 32-byte sector for 16-byte entries).
+// A 1-indexed binary heap whose entries 1..topn live in shared memory and the
+// rest in global memory (the global array keeps the same indices).  The two
+// children 2i, 2i+1 of a node are adjacent.
+template <class P> struct HeapRef {
+    using E = typename P::Entry;
+    E *g;          // global array, index 0 unused
+    E *s;          // shared top, index 0 unused
+    uint32_t topn; // entries held in shared memory
+    __device__ __forceinline__ E ld(uint32_t i) const { return i <= topn ? s[i] : P::load(g + i); }
+    __device__ __forceinline__ void st(uint32_t i, const E &v) const {
+        if (i <= topn)
+            s[i] = v;
+        else
+            P::store(g + i, v);
+    }
+};
+
 template <class P>
-__device__ __forceinline__ bool heap_pop(typename P::Entry *hp, uint32_t &size,
-                                         typename P::Entry &out) {
+__device__ __forceinline__ bool heap_pop(const HeapRef<P> &h, uint32_t &size, typename P::Entry &out) {
     using E = typename P::Entry;
     if (size == 0) return false;
-    out = P::load(hp + 1);
-    const E last = P::load(hp + size);
+    out = h.ld(1);
+    const E last = h.ld(size);
     size -= 1;
     if (size == 0) return true;
     uint32_t now = 1;
     for (;;) {
         uint32_t c = now << 1;
         if (c > size) break;
-        E a = P::load(hp + c);
+        E a = h.ld(c);
         if (c < size) {
-            const E b = P::load(hp + c + 1);
+            const E b = h.ld(c + 1);
             if (P::less(b, a)) {
                 a = b;
                 ++c;
             }
         }
         if (!P::less(a, last)) break;
-        P::store(hp + now, a);
+        h.st(now, a);
         now = c;
     }
-    P::store(hp + now, last);
+    h.st(now, last);
     return true;
 }
 
 template <class P>
-__device__ __forceinline__ void heap_push(typename P::Entry *hp, uint32_t &size,
-                                          const typename P::Entry &v) {
+__device__ __forceinline__ void heap_push(const HeapRef<P> &h, uint32_t &size, const typename P::Entry &v) {
     using E = typename P::Entry;
     uint32_t now = ++size;
     while (now > 1) {
         const uint32_t par = now >> 1;
-        const E pv = P::load(hp + par);
+        const E pv = h.ld(par);
         if (!P::less(v, pv)) break;
-        P::store(hp + now, pv);
+        h.st(now, pv);
         now = par;
     }
-    P::store(hp + now, v);
+    h.st(now, v);
 }
 
 // ---------------------------------------------------------- cost minima ---
@@ -143,6 +163,62 @@ __device__ __forceinline__ bool atomic_min_cost(unsigned long long *addr, uint64
     return false;
 }
 
+// (key, g) half of a slot, updated as one 16-byte word.
+struct __align__(16) KeyG {
+    unsigned long long key, g;
+};
+__device__ __forceinline__ KeyG cas128(Slot *s, KeyG cmp, KeyG val) {
+    return atomicCAS(reinterpret_cast<KeyG *>(s), cmp, val);
+}
+
+enum : int { RELAX_NONE = 0, RELAX_IMPROVED = 1, RELAX_INSERTED = 3, RELAX_FULL = 4 };
+
+// Find-or-insert `key` and lower its g to `g` in one pass.  The home slot is
+// tried with a single 16-byte CAS that either claims it empty with (key, g)
+// or returns what it holds; later probe steps read first and only CAS a slot
+// that is empty or holds the key.  Returns RELAX_INSERTED (new slot, g set),
+// RELAX_IMPROVED (existing slot, g strictly lowered), RELAX_NONE (existing
+// slot, g not better) or RELAX_FULL (probe limit).
+template <class P>
+__device__ __forceinline__ int relax(Slot *tab, uint64_t mask, uint32_t max_probe, uint64_t key, uint64_t g,
+                                     uint32_t *slot_out) {
+    uint64_t h = mix64(key) & mask;
+    const KeyG empty{kEmptyKey, kInfCost};
+    for (uint32_t i = 0; i < max_probe; ++i) {
+        KeyG cur;
+        if (i == 0) {
+            cur = cas128(tab + h, empty, KeyG{key, g});
+            if (cur.key == kEmptyKey) {
+                *slot_out = (uint32_t)h;
+                return RELAX_INSERTED;
+            }
+        } else {
+            const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(tab + h));
+            cur.key = v.x;
+            cur.g = v.y;
+            if (cur.key == kEmptyKey) {
+                cur = cas128(tab + h, empty, KeyG{key, g});
+                if (cur.key == kEmptyKey) {
+                    *slot_out = (uint32_t)h;
+                    return RELAX_INSERTED;
+                }
+            }
+        }
+        if (cur.key == key) {
+            *slot_out = (uint32_t)h;
+            // lower g; the key half never changes once set
+            while (P::cost_cmp(g, cur.g) < 0) {
+                const KeyG old = cas128(tab + h, cur, KeyG{key, g});
+                if (old.key == cur.key && old.g == cur.g) return RELAX_IMPROVED;
+                cur = old;
+            }
+            return RELAX_NONE;
+        }
+        h = (h + 1) & mask;
+    }
+    return RELAX_FULL;
+}
+
 __device__ __forceinline__ Cand load_cand(const Cand *p) {
     const uint4 a = __ldcg(reinterpret_cast<const uint4 *>(p));
     const uint4 b = __ldcg(reinterpret_cast<const uint4 *>(p) + 1);
@@ -156,115 +232,165 @@ __device__ __forceinline__ Cand load_cand(const Cand *p) {
     return c;
 }
 
+// Shared-memory layout of one CTA of a search team.
+struct PopInfo {
+    unsigned long long key, g;
+    uint32_t aux, slot, mask, excl;  // excl: exclusive prefix of successor counts
+};
+
+template <class P> struct SearchSmem {
+    // pops, heap tops, then a small scratch area (warp totals)
+    static __host__ __device__ size_t scratch_offset(uint32_t H, uint32_t topn) {
+        return ((size_t)H * sizeof(PopInfo) + (size_t)H * (topn + 1) * sizeof(typename P::Entry) + 15) & ~(size_t)15;
+    }
+    static __host__ __device__ size_t bytes(uint32_t H, uint32_t topn) {
+        return scratch_offset(H, topn) + 4 * (2 + (H + 31) / 32);
+    }
+};
+
 // ------------------------------------------------------------ the search ---
 // Runs up to `budget` rounds (resumable: state lives in TeamState, the heaps
 // and the table).  Returns ST_RUNNING if the budget ran out first, else the
-// final status.  Every team thread must call it.
+// final status.  Every thread of every CTA of the team must call it with the
+// same H (heaps per CTA, 1 <= H <= blockDim.x) and topn; `smem` points at
+// SearchSmem<P>::bytes(H, topn) bytes of shared memory.
 template <class P, class Team>
-__device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typename P::Entry> &m,
-                              uint64_t budget) {
+__device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typename P::Entry> &m, uint32_t H,
+                              uint32_t topn, unsigned char *smem, uint64_t budget) {
     using E = typename P::Entry;
     TeamState *st = team.st;
-    const uint32_t k = team.size(), rank = team.rank();
-    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t T = blockDim.x, tid = threadIdx.x, lane = tid & 31u;
+    const uint32_t C = team.ctas(), cta = team.cta();
+    const bool owner = tid < H;
+    const uint32_t myh = cta * H + tid;  // global heap index (valid when owner)
+
+    PopInfo *pop = reinterpret_cast<PopInfo *>(smem);
+    E *tops = reinterpret_cast<E *>(smem + (size_t)H * sizeof(PopInfo));
+    uint32_t *scratch = reinterpret_cast<uint32_t *>(smem + SearchSmem<P>::scratch_offset(H, topn));
+
+    HeapRef<P> myheap{m.heaps + (size_t)(owner ? myh : 0) * m.stride, tops + (size_t)(owner ? tid : 0) * (topn + 1),
+                      topn};
     uint64_t nE = 0, nS = 0, nP = 0;
 
     if (team.rd32(&st->started) == 0) {
-        if (rank == 0) {
+        if (cta == 0 && tid == 0) {
             const uint64_t key0 = prob.start_key();
+            const uint32_t aux0 = prob.start_aux();
             uint32_t s0;
-            if (find_or_insert(m.tab, m.mask, key0, m.max_probe, &s0) == FIND_FULL) {
+            if (relax<P>(m.tab, m.mask, m.max_probe, key0, 0, &s0) == RELAX_FULL) {
                 set_error(&st->error, ST_HASH_FULL);
             } else {
-                const uint32_t aux0 = prob.start_aux();
-                m.tab[s0].g = 0;
                 m.tab[s0].aux = aux0;
                 m.tab[s0].prev = kNone;
                 uint32_t sz = 0;
-                heap_push<P>(m.heaps, sz, prob.make_entry(prob.f_of(key0, 0, aux0), 0, s0));
-                m.heap_size[0] = sz;
+                heap_push<P>(myheap, sz, prob.make_entry(prob.f_of(key0, 0, aux0), 0, s0));
+                m.heap_size[myh] = sz;
                 st->inserted = 1;
             }
             st->started = 1;
         }
         team.sync();
+    } else if (owner) {
+        // resuming: bring the shared top of this heap back from global memory
+        const uint32_t sz = ldcg_u32(&m.heap_size[myh]);
+        for (uint32_t i = 1; i <= topn && i <= sz; ++i) myheap.s[i] = P::load(myheap.g + i);
     }
+    __syncthreads();
 
     uint32_t base = team.rd32(&st->base);
     uint64_t round = team.rd64(&st->round);
     uint32_t status = ST_RUNNING;
-    E *const myheap = m.heaps + (size_t)rank * m.stride;
+    uint32_t hs = owner ? ldcg_u32(&m.heap_size[myh]) : 0;  // this owner's heap size (private)
+    const uint32_t owner_warps = (H + 31u) / 32u;
 
     for (uint64_t it = 0;; ++it) {
         const uint32_t par = (uint32_t)(round & 1);
 
-        // ---------------------------------------------------- phase 1 ---
-        E e;
-        uint32_t hs = ldcg_u32(&m.heap_size[rank]);
-        bool have = false;
-        if (hs) {
-            have = heap_pop<P>(myheap, hs, e);
-            m.heap_size[rank] = hs;
-        }
-        const uint64_t ecost = have ? P::entry_cost(e) : kInfCost;
-        const uint64_t wmin = warp_min_cost<P>(ecost);
-        if (lane == 0 && wmin != kInfCost) atomic_min_cost<P>(&st->round_min[par], wmin);
-
-        uint64_t key = 0, g = 0;
-        uint32_t aux = 0, pslot = 0, mv = 0;
-        if (have) {
-            pslot = e.slot;
-            P::load_node(m.tab + pslot, key, g, aux);
-            const uint64_t fcur = prob.f_of(key, g, aux);
-            if (fcur != ecost) {
-                // stale: the node was improved after this entry was pushed
-            } else if (prob.is_goal(key)) {
-                atomic_min_cost<P>(&st->goal_best, fcur);
-                st->goal_slot = pslot;  // every goal pop names the same slot
-            } else {
-                ++nE;
-                mv = prob.moves(key, aux);
+        // ------------------------------------------------ phase 1: pop ---
+        if (tid < owner_warps * 32u) {  // warps holding heap owners
+            E e;
+            uint32_t mv = 0;
+            const bool have = owner && heap_pop<P>(myheap, hs, e);
+            const uint64_t ecost = have ? P::entry_cost(e) : kInfCost;
+            const uint64_t wmin = warp_min_cost<P>(ecost);
+            if (lane == 0 && wmin != kInfCost) atomic_min_cost<P>(&st->round_min[par], wmin);
+            if (have) {
+                uint64_t key, g;
+                uint32_t aux;
+                P::load_node(m.tab + e.slot, key, g, aux);
+                const uint64_t fcur = prob.f_of(key, g, aux);
+                if (fcur != ecost) {
+                    // stale: the node was improved after this entry was pushed
+                } else if (prob.is_goal(key)) {
+                    atomic_min_cost<P>(&st->goal_best, fcur);
+                    st->goal_slot = e.slot;  // every goal pop names the same slot
+                } else {
+                    ++nE;
+                    mv = prob.moves(key, aux);
+                    pop[tid].key = key;
+                    pop[tid].g = g;
+                    pop[tid].aux = aux;
+                    pop[tid].slot = e.slot;
+                }
             }
-        }
-
-        // Spread the warp's successors over its lanes.
-        const uint32_t cnt = __popc(mv);
-        uint32_t incl = cnt;
+            // exclusive prefix of successor counts: within the warp here,
+            // warp offsets added after the barrier
+            const uint32_t cnt = __popc(mv);
+            uint32_t incl = cnt;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t t = __shfl_up_sync(kFull, incl, o);
-            if (lane >= (uint32_t)o) incl += t;
-        }
-        const uint32_t total = __shfl_sync(kFull, incl, 31);
-        const uint32_t excl = incl - cnt;
-        for (uint32_t b0 = 0; b0 < total; b0 += 32) {
-            const uint32_t j = b0 + lane;
-            // owner = largest lane whose exclusive prefix is <= j (it has cnt > 0)
-            uint32_t owner = 0;
-#pragma unroll
-            for (int s = 16; s > 0; s >>= 1) {
-                const uint32_t ex = __shfl_sync(kFull, excl, owner + s);
-                if (ex <= j) owner += s;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(kFull, incl, o);
+                if (lane >= (uint32_t)o) incl += t;
             }
-            const uint32_t kth = j - __shfl_sync(kFull, excl, owner);
-            const uint32_t omask = __shfl_sync(kFull, mv, owner);
-            const uint64_t okey = shfl64(key, owner), og = shfl64(g, owner);
-            const uint32_t oaux = __shfl_sync(kFull, aux, owner);
-            const uint32_t oslot = __shfl_sync(kFull, pslot, owner);
+            if (owner) {
+                pop[tid].mask = mv;
+                pop[tid].excl = incl - cnt;
+            }
+            if (lane == 31) scratch[2 + (tid >> 5)] = incl;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t acc = 0;
+            for (uint32_t w = 0; w < owner_warps; ++w) {
+                const uint32_t t = scratch[2 + w];
+                scratch[2 + w] = acc;
+                acc += t;
+            }
+            scratch[0] = acc;
+        }
+        __syncthreads();
+        if (owner) pop[tid].excl += scratch[2 + (tid >> 5)];
+        const uint32_t total = scratch[0];
+        __syncthreads();
+
+        // ----------------------------------- phase 1: relax successors ---
+        for (uint32_t b0 = 0; b0 < total; b0 += T) {
+            const uint32_t j = b0 + tid;
             bool improved = false, inserted = false;
-            uint32_t nslot = 0, naux = 0;
+            uint32_t nslot = 0, naux = 0, oslot = 0;
             uint64_t ng = 0, nf = 0;
             if (j < total) {
-                const int move = (int)__fns(omask, 0, (int)kth + 1);
+                // source pop = largest h with excl[h] <= j (it has a successor)
+                uint32_t lo = 0, hi = H - 1;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi + 1) >> 1;
+                    if (pop[mid].excl <= j)
+                        lo = mid;
+                    else
+                        hi = mid - 1;
+                }
+                const PopInfo &pi = pop[lo];
+                const int move = (int)__fns(pi.mask, 0, (int)(j - pi.excl) + 1);
+                oslot = pi.slot;
                 uint64_t nkey;
-                prob.apply(okey, og, oaux, move, nkey, ng, naux, nf);
+                prob.apply(pi.key, pi.g, pi.aux, move, nkey, ng, naux, nf);
                 ++nS;
-                const int r = find_or_insert(m.tab, m.mask, nkey, m.max_probe, &nslot);
-                if (r == FIND_FULL) {
+                const int r = relax<P>(m.tab, m.mask, m.max_probe, nkey, ng, &nslot);
+                if (r == RELAX_FULL) {
                     set_error(&st->error, ST_HASH_FULL);
                 } else {
-                    inserted = (r == FIND_INSERTED);
-                    improved = atomic_min_cost<P>(&m.tab[nslot].g, ng);
+                    inserted = (r == RELAX_INSERTED);
+                    improved = (r & RELAX_IMPROVED) != 0;
                 }
             }
             const uint32_t ib = __ballot_sync(kFull, inserted);
@@ -295,12 +421,11 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
 
         // -------------------------------------------------- decision ---
         // Every value read here is written only before the barrier above or
-        // after the next one, so all threads decide alike.
+        // after the next one, so all threads decide alike.  Phase-2 errors of
+        // round r are written to error2[r & 1] and read at the decision of
+        // round r + 1.
         const uint64_t rmin = team.rd64(&st->round_min[par]);
         const uint64_t gbest = team.rd64(&st->goal_best);
-        // Phase-2 errors of round r are written to error2[r & 1] and read at
-        // the decision of round r + 1, so no thread can see one that another
-        // thread of the same decision missed.
         uint32_t err = team.rd32(&st->error);
         if (!err) err = team.rd32(&st->error2[par ^ 1]);
         const uint32_t ncand = team.rd32(&st->cand_count[par]);
@@ -323,35 +448,39 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         }
 
         // ---------------------------------------------------- phase 2 ---
-        if (rank == 0) {
+        if (cta == 0 && tid == 0) {
             st->round_min[par ^ 1] = kInfCost;
             st->cand_count[par ^ 1] = 0;
         }
-        const uint32_t target = (rank + base) % k;
-        base = (uint32_t)(((uint64_t)base + ncand) % k);
-        if (rank < ncand) {
-            E *th = m.heaps + (size_t)target * m.stride;
-            uint32_t ths = ldcg_u32(&m.heap_size[target]);
-            for (uint32_t i = rank; i < ncand; i += k) {
+        if (owner) {
+            // This CTA's share of the round's candidates is every C-th one
+            // (a contiguous chunk would hold the successors of a few warps'
+            // pops, i.e. one small region of the search, and starve the rest
+            // of the team's heaps of it); the share is dealt over its heaps.
+            for (uint32_t i = cta + C * ((tid + base) % H); i < ncand; i += C * H) {
                 const Cand c = load_cand(m.cand + i);
                 if (ldcg_u64(&m.tab[c.slot].g) != c.g) continue;  // lost to a better writer
                 m.tab[c.slot].prev = c.parent;
                 m.tab[c.slot].aux = c.aux;
-                if (ths + 1 >= m.stride) {
+                if (hs + 1 >= m.stride) {
                     set_error(&st->error2[par], ST_HEAP_OVERFLOW);
                     break;
                 }
-                heap_push<P>(th, ths, prob.make_entry(c.f, c.g, c.slot));
+                heap_push<P>(myheap, hs, prob.make_entry(c.f, c.g, c.slot));
                 ++nP;
             }
-            m.heap_size[target] = ths;
         }
+        base = (uint32_t)(((uint64_t)base + ncand) % H);
         team.sync();
         if (it + 1 >= budget) break;
     }
 
-    // Persist the resumable state (uniform values; rank 0 writes).
-    if (rank == 0) {
+    // Persist the resumable state.
+    if (owner) {
+        m.heap_size[myh] = hs;
+        for (uint32_t i = 1; i <= topn && i <= hs; ++i) P::store(myheap.g + i, myheap.s[i]);
+    }
+    if (cta == 0 && tid == 0) {
         st->round = round;
         st->base = base;
         if (status != ST_RUNNING) st->status = status;

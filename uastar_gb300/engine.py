@@ -200,10 +200,10 @@ class Engine:
 
     def __init__(self, ordinal: int = 0, *, heaps: int = 0, block_threads: int = 0, heap_capacity: int = 0,
                  hash_log2_slots: int = 0, max_load: float = 0.0, max_rounds: int = 0,
-                 wait_timeout_s: float = 0.0):
+                 wait_timeout_s: float = 0.0, threads_per_heap: int = 0, heap_top_levels: int = 0):
         self._lib = L.load()
         cfg = L.Config(heaps, block_threads, heap_capacity, hash_log2_slots, max_load, max_rounds,
-                       wait_timeout_s)
+                       wait_timeout_s, threads_per_heap, heap_top_levels)
         self._h = self._lib.uastar_create(ordinal, C.byref(cfg))
         if not self._h:
             raise EngineError(L.CUDA_ERROR, f"cannot create an engine on CUDA device {ordinal}")
@@ -310,13 +310,13 @@ class Engine:
         return out.tolist()
 
     # batched engine
-    def batch_solve(self, instances: Iterable, *, threads_per_instance: int = 0, heap_capacity: int = 0,
-                    load_factor: float = 0.0, ctas: int = 0, use_graph: int = 1):
+    def batch_solve(self, instances: Iterable, *, threads_per_instance: int = 0, threads_per_heap: int = 0,
+                    heap_capacity: int = 0, load_factor: float = 0.0, ctas: int = 0, use_graph: int = 1):
         insts = list(instances)
         keep: list = []
         arr = (L.Instance * max(1, len(insts)))(*[_to_struct(i, keep) for i in insts])
         res = (L.InstanceResult * max(1, len(insts)))()
-        cfg = L.BatchConfig(threads_per_instance, heap_capacity, load_factor, ctas, use_graph)
+        cfg = L.BatchConfig(threads_per_instance, threads_per_heap, heap_capacity, load_factor, ctas, use_graph)
         st = L.BatchStats()
         self._check(self._lib.uastar_batch_solve(self._h, arr, len(insts), C.byref(cfg), res, C.byref(st)),
                     "batch_solve")
@@ -333,9 +333,10 @@ class Engine:
 
     # serving loop
     def serve_start(self, *, hbm_budget_gb: float = 120.0, slots: int = 0, threads_per_instance: int = 0,
-                    heap_capacity: int = 0, rounds_per_quantum: int = 0, load_factor: float = 0.0) -> None:
-        cfg = L.ServeConfig(hbm_budget_gb, slots, threads_per_instance, heap_capacity, rounds_per_quantum,
-                            load_factor)
+                    threads_per_heap: int = 0, heap_capacity: int = 0, rounds_per_quantum: int = 0,
+                    load_factor: float = 0.0) -> None:
+        cfg = L.ServeConfig(hbm_budget_gb, slots, threads_per_instance, threads_per_heap, heap_capacity,
+                            rounds_per_quantum, load_factor)
         self._check(self._lib.uastar_serve_start(self._h, C.byref(cfg)), "serve_start")
 
     def serve_submit(self, inst, arrival_s: float = 0.0) -> int:
