@@ -61,7 +61,7 @@ typedef struct {
     int32_t block_threads;   /* CTA size of the plain engine's persistent kernel (0 -> 256) */
     int32_t heap_capacity;   /* entries per heap (0 -> auto, grown on overflow) */
     int32_t hash_log2_slots; /* dedup table = 2^n slots of 32 B (0 -> auto from instance) */
-    double max_load;         /* dedup table load limit in (0,1) (0 -> 0.9) */
+    double max_load;         /* dedup table load limit in (0,1) (0 -> 0.8) */
     int64_t max_rounds;      /* GA* round limit per solve (0 -> 2^31) */
     double wait_timeout_s;   /* bound on any device-side barrier wait (0 -> 10 s) */
     int32_t threads_per_heap; /* threads that share one heap's successors (0 -> 4 grid, 2 puzzle) */

@@ -34,7 +34,8 @@ def drain(eng, n, timeout=120.0):
 
 
 def test_stream_results_equal_alone_and_in_mix(seng):
-    stream = WL.serve_stream(60, rate_per_s=400.0, max_side=1024)
+    # moderate instances: every one fits the 16 GB budget of this test
+    stream = WL.serve_stream(60, rate_per_s=400.0, max_side=1024, walks=(20, 90), min_side=64)
     insts = [s.instance() for _, s in stream]
     seng.serve_start(hbm_budget_gb=16.0, slots=32, rounds_per_quantum=64)
     t0 = WL.E.now_s() + 0.05

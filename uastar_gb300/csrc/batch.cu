@@ -21,6 +21,8 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <cstdio>
+#include <cstdlib>
 #include <ctime>
 #include <numeric>
 #include <vector>
@@ -42,9 +44,9 @@ struct InstDesc {
     uint32_t log2_slots;
     uint32_t fresh;       // serving: state not yet initialised
     uint64_t max_rounds;
-    uint64_t heap_off16;  // serving: first 16-byte entry of this request's heap slice
-    uint32_t heap_stride16;  // serving: entries per heap of that slice
-    uint32_t pad;
+    uint64_t heap_off;    // serving: byte offset of this request's heap slice
+    uint32_t heap_stride; // serving: entries per heap of that slice
+    uint32_t heap_hcap;   // serving: maximum heap size
 };
 
 struct InstOut {
@@ -61,15 +63,18 @@ struct BatchArgs {
     const uint8_t *pdb3;
     const uint8_t *pdb4;
     Slot *tab;
-    uint8_t *heaps;        // per CTA: H heaps x stride16 x 16 bytes
-    uint32_t stride16;     // heap stride in 16-byte entries (puzzles use 2x as 8-byte entries)
+    uint8_t *heaps;        // per CTA: H heaps x slice bytes
+    uint64_t slice;        // bytes per heap (batch)
     uint32_t *hsize;       // per CTA: H
     Cand *cand;            // per CTA: H * 8
     uint32_t H;            // heaps per instance (CTA)
-    uint32_t topn_grid;    // heap entries kept in shared memory (grid / puzzle entry sizes)
-    uint32_t topn_puzzle;
+    uint32_t L_grid, L_puzzle;            // heap levels in shared memory
+    uint32_t stride_grid, stride_puzzle;  // batch heap geometry per entry type
+    uint32_t hcap_grid, hcap_puzzle;
     InstOut *outs;
     TeamState *states;     // serving: per slot persisted team state
+    TeamState *cstates;    // cluster teams: per cluster team state
+    uint32_t *cnext;       // cluster teams: instance index broadcast per cluster
     double max_load;
     uint64_t budget;       // rounds per call (serving quantum) or ~0
     int serving;           // 1: CTA b serves slot b; 0: work queue
@@ -90,12 +95,12 @@ __device__ void init_state(TeamState *st) {
 }
 
 // Runs one instance on this CTA for up to `budget` rounds.
-__device__ uint32_t run_instance(const BatchArgs &a, const InstDesc &d, TeamState *st, uint8_t *heaps,
-                                 uint32_t stride16, uint32_t *hs, Cand *cand, unsigned char *smem,
-                                 uint64_t budget) {
-    BlockTeam team{st};
+template <class Team>
+__device__ uint32_t run_instance(const BatchArgs &a, const InstDesc &d, Team &team, uint8_t *heaps,
+                                 uint32_t *hs, Cand *cand, unsigned char *smem, uint64_t budget) {
     Slot *tab = a.tab + d.tab_off;
     const uint64_t slots = 1ull << d.log2_slots;
+    const bool own_geo = a.serving != 0;  // serving requests carry their heap geometry
     if (d.kind == UASTAR_KIND_GRID) {
         GridProblem prob;
         prob.bm = a.bitmaps + d.bm_word;
@@ -106,37 +111,37 @@ __device__ uint32_t run_instance(const BatchArgs &a, const InstDesc &d, TeamStat
         prob.ex = d.ex;
         prob.ey = d.ey;
         SearchMem<GridEntry> m{tab, slots - 1, (uint64_t)(slots * a.max_load), 4096u,
-                               reinterpret_cast<GridEntry *>(heaps), stride16, hs, cand, d.max_rounds};
-        return ga_search(prob, team, m, a.H, a.topn_grid, smem, budget);
+                               reinterpret_cast<GridEntry *>(heaps),
+                               own_geo ? d.heap_stride : a.stride_grid, own_geo ? d.heap_hcap : a.hcap_grid,
+                               a.L_grid, hs, cand, d.max_rounds};
+        return ga_search(prob, team, m, a.H, smem, budget);
     }
+    SearchMem<PuzzleEntry> m{tab, slots - 1, (uint64_t)(slots * a.max_load), 4096u,
+                             reinterpret_cast<PuzzleEntry *>(heaps),
+                             own_geo ? d.heap_stride : a.stride_puzzle, own_geo ? d.heap_hcap : a.hcap_puzzle,
+                             a.L_puzzle, hs, cand, d.max_rounds};
     if (d.n == 4) {
         PuzzleProblem<4> prob;
         prob.pdb = a.pdb4;
         prob.start = d.start_key;
         prob.goal = PuzzleProblem<4>::goal_key();
-        SearchMem<PuzzleEntry> m{tab, slots - 1, (uint64_t)(slots * a.max_load), 4096u,
-                                 reinterpret_cast<PuzzleEntry *>(heaps), stride16 * 2, hs, cand,
-                                 d.max_rounds};
-        return ga_search(prob, team, m, a.H, a.topn_puzzle, smem, budget);
+        return ga_search(prob, team, m, a.H, smem, budget);
     }
     PuzzleProblem<3> prob;
     prob.pdb = a.pdb3;
     prob.start = d.start_key;
     prob.goal = PuzzleProblem<3>::goal_key();
-    SearchMem<PuzzleEntry> m{tab, slots - 1, (uint64_t)(slots * a.max_load), 4096u,
-                             reinterpret_cast<PuzzleEntry *>(heaps), stride16 * 2, hs, cand, d.max_rounds};
-    return ga_search(prob, team, m, a.H, a.topn_puzzle, smem, budget);
+    return ga_search(prob, team, m, a.H, smem, budget);
 }
 
 __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
     __shared__ TeamState st;
     __shared__ uint32_t s_next;
-    extern __shared__ __align__(16) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem[];
     const uint32_t H = a.H;
     // batch: each CTA owns a heap slice reused by the instances it takes;
     // serving: each request owns a slice named by its descriptor
-    uint8_t *heaps = a.heaps + (size_t)blockIdx.x * H * a.stride16 * 16;
-    uint32_t stride16 = a.stride16;
+    uint8_t *heaps = a.heaps + (size_t)blockIdx.x * H * a.slice;
     uint32_t *hs = a.hsize + (size_t)blockIdx.x * H;
     Cand *cand = a.cand + (size_t)blockIdx.x * H * 8;
     for (uint32_t iter = 0;; ++iter) {
@@ -152,19 +157,18 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
         const InstDesc d = a.descs[i];
         if (a.serving && d.kind == 0) break;  // empty serving slot
         const unsigned long long t_start = globaltimer_ns();
-        if (a.serving) {
-            heaps = a.heaps + d.heap_off16 * 16;
-            stride16 = d.heap_stride16;
-        }
+        if (a.serving) heaps = a.heaps + d.heap_off;
         if (!a.serving || d.fresh) {
-            clear_partition(a.tab + d.tab_off, 1ull << d.log2_slots);
+            // serving partitions are cleared by the host at admission (fresh == 2)
+            if (d.fresh != 2) clear_partition(a.tab + d.tab_off, 1ull << d.log2_slots);
             for (uint32_t j = threadIdx.x; j < H; j += blockDim.x) hs[j] = 0;
             if (threadIdx.x == 0) init_state(&st);
         } else if (threadIdx.x == 0) {
             st = a.states[i];
         }
         __syncthreads();
-        run_instance(a, d, &st, heaps, stride16, hs, cand, smem, a.budget);
+        BlockTeam team{&st};
+        run_instance(a, d, team, heaps, hs, cand, smem, a.budget);
         __syncthreads();
         if (threadIdx.x == 0) {
             InstOut o;
@@ -185,6 +189,59 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
             if (a.serving) a.states[i] = st;
         }
         __syncthreads();
+    }
+}
+
+__device__ void clear_partition_team(Slot *tab, uint64_t slots, uint32_t rank, uint32_t nranks) {
+    uint4 *p = reinterpret_cast<uint4 *>(tab);
+    const uint4 v = make_uint4(~0u, ~0u, ~0u, ~0u);
+    for (uint64_t j = (uint64_t)rank * blockDim.x + threadIdx.x; j < slots * 2; j += (uint64_t)nranks * blockDim.x)
+        p[j] = v;
+}
+
+// Batch of large instances: one thread-block cluster per instance.  The
+// cluster's CTAs are one GA* team (H heaps each); instances come from the
+// device work queue, one per cluster at a time.
+__global__ void __launch_bounds__(512, 1) k_batch_cluster(BatchArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const uint32_t crank = ClusterTeam{nullptr}.cta(), csize = ClusterTeam{nullptr}.ctas();
+    const uint32_t cid = blockIdx.x / csize;
+    const uint32_t H = a.H;
+    TeamState *st = a.cstates + cid;
+    ClusterTeam team{st};
+    uint8_t *heaps = a.heaps + (size_t)cid * csize * H * a.slice;
+    uint32_t *hs = a.hsize + (size_t)cid * csize * H;
+    Cand *cand = a.cand + (size_t)cid * csize * H * 8;
+    for (;;) {
+        if (crank == 0 && threadIdx.x == 0) a.cnext[cid] = atomicAdd(a.queue, 1u);
+        team.sync();
+        const uint32_t i = ldcg_u32(&a.cnext[cid]);
+        if (i >= a.count) break;
+        const InstDesc d = a.descs[i];
+        const unsigned long long t_start = globaltimer_ns();
+        clear_partition_team(a.tab + d.tab_off, 1ull << d.log2_slots, crank, csize);
+        for (uint32_t j = threadIdx.x; j < H; j += blockDim.x) hs[crank * H + j] = 0;
+        if (crank == 0 && threadIdx.x == 0) init_state(st);
+        team.sync();
+        run_instance(a, d, team, heaps, hs, cand, smem, a.budget);
+        team.sync();
+        if (crank == 0 && threadIdx.x == 0) {
+            InstOut o;
+            o.status = ldcg_u32(&st->status);
+            o.goal_slot = ldcg_u32(&st->goal_slot);
+            o.goal_best = ldcg_u64(&st->goal_best);
+            o.rounds = ldcg_u64(&st->round);
+            o.expanded = ldcg_u64(&st->expanded);
+            o.generated = ldcg_u64(&st->generated);
+            o.pushed = ldcg_u64(&st->pushed);
+            o.inserted = ldcg_u64(&st->inserted);
+            o.t_start = t_start;
+            o.t_end = globaltimer_ns();
+            const uint32_t e1 = ldcg_u32(&st->error), e20 = ldcg_u32(&st->error2[0]), e21 = ldcg_u32(&st->error2[1]);
+            if (o.status == ST_RUNNING && (e1 || e20 || e21)) o.status = e1 ? e1 : (e20 ? e20 : e21);
+            a.outs[i] = o;
+        }
+        team.sync();
     }
 }
 
@@ -210,6 +267,16 @@ __global__ void k_batch_walk(const InstDesc *descs, const InstOut *outs, const u
 }  // namespace uastar
 
 namespace {
+
+// UASTAR_DEBUG=1 in the environment prints the batch engine's wave plan and
+// timings to stderr.
+bool debug_log() {
+    static const bool on = [] {
+        const char *v = std::getenv("UASTAR_DEBUG");
+        return v && *v && *v != '0';
+    }();
+    return on;
+}
 
 inline double now_ms() {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch())
@@ -249,10 +316,12 @@ bool board_solvable(int n, const uint8_t *tiles) {
 // Estimated dedup nodes of an instance (a sizing hint; overflow is retried).
 uint64_t est_nodes(const uastar_instance &in) {
     if (in.est_nodes > 0) return (uint64_t)in.est_nodes;
-    if (in.kind == UASTAR_KIND_GRID) return std::max<uint64_t>(4096, (uint64_t)in.H * in.W / 4);
-    // Puzzles start small; an instance that fills its partition is re-run
-    // in the next wave with 8x the space.
-    return in.n == 3 ? 32768 : 65536;
+    // Grids: an eighth of the cells (random grids searched corner to corner
+    // touch a few percent to ~20 %).  Puzzles: 2^17 states (the median 15-puzzle
+    // of 60-300 random moves needs ~2e5 expansions).  An instance that fills
+    // its partition is re-run in the next wave with 16x the space.
+    if (in.kind == UASTAR_KIND_GRID) return std::max<uint64_t>(4096, (uint64_t)in.H * in.W / 8);
+    return in.n == 3 ? 65536 : 262144;
 }
 
 struct BatchPlan {
@@ -282,19 +351,30 @@ int32_t check_instance(const uastar_instance &in) {
 
 struct BatchGeometry {
     int T, ctas;
-    uint32_t H, topn_grid, topn_puzzle;
-    uint32_t stride16;
+    int csize = 0;      // > 0: cluster teams of csize CTAs (ctas = clusters * csize)
+    uint32_t H, L_grid, L_puzzle;
+    uint64_t want;  // requested heap capacity (entries)
+    HeapGeometry<GridProblem> hg_grid;
+    HeapGeometry<PuzzleProblem<4>> hg_puzzle;
+    uint64_t slice;  // bytes per heap
     size_t smem;
     double load;
+    void set_capacity(uint64_t w) {
+        want = w;
+        hg_grid = heap_geometry<GridProblem>(L_grid, w);
+        hg_puzzle = heap_geometry<PuzzleProblem<4>>(L_puzzle, w);
+        slice = std::max<uint64_t>((uint64_t)hg_grid.stride * sizeof(GridEntry),
+                                   (uint64_t)hg_puzzle.stride * sizeof(PuzzleEntry));
+        slice = (slice + 127) & ~127ull;
+    }
 };
 
-// Largest 2^L - 1 heap-top entries per heap whose shared memory fits `budget`.
+// Largest L (>= 1) whose shared heap tops fit `budget`.
 template <class P> uint32_t fit_top(uint32_t H, size_t budget) {
-    uint32_t best = 0;
-    for (int L = 1; L <= 10; ++L) {
-        const uint32_t topn = (1u << L) - 1;
-        if (SearchSmem<P>::bytes(H, topn) > budget) break;
-        best = topn;
+    uint32_t best = 1;
+    for (uint32_t L = 1; L <= 10; ++L) {
+        if (SearchSmem<P>::bytes(H, L) > budget) break;
+        best = L;
     }
     return best;
 }
@@ -308,10 +388,11 @@ int32_t resolve_block_geometry(uastar_engine *eng, int threads, int tph, BatchGe
     int smem_sm = 0;
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, eng->device);
     const size_t per_cta = (size_t)std::max(16 * 1024, smem_sm / 2 - 4 * 1024);
-    g->topn_grid = fit_top<GridProblem>(g->H, per_cta);
-    g->topn_puzzle = fit_top<PuzzleProblem<4>>(g->H, per_cta);
-    g->smem = std::max(SearchSmem<GridProblem>::bytes(g->H, g->topn_grid),
-                       SearchSmem<PuzzleProblem<4>>::bytes(g->H, g->topn_puzzle));
+    g->L_grid = fit_top<GridProblem>(g->H, per_cta);
+    g->L_puzzle = fit_top<PuzzleProblem<4>>(g->H, per_cta);
+    g->smem = std::max(SearchSmem<GridProblem>::bytes(g->H, g->L_grid),
+                       SearchSmem<PuzzleProblem<4>>::bytes(g->H, g->L_puzzle));
+    g->set_capacity(4095);
     cudaError_t e = cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g->smem);
     if (e != cudaSuccess) return fail_cuda(eng, e, "smem attribute");
     int occ = 0;
@@ -321,12 +402,39 @@ int32_t resolve_block_geometry(uastar_engine *eng, int threads, int tph, BatchGe
     return UASTAR_OK;
 }
 
+// Cluster teams: the same CTA geometry, `csize` CTAs per team, as many
+// teams as can be co-resident.
+int32_t resolve_cluster_geometry(uastar_engine *eng, int csize, BatchGeometry *g) {
+    cudaError_t e = cudaFuncSetAttribute(k_batch_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g->smem);
+    if (e == cudaSuccess && csize > 8)
+        e = cudaFuncSetAttribute(k_batch_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return fail_cuda(eng, e, "cluster attributes");
+    cudaLaunchConfig_t lc = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)csize;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    lc.gridDim = dim3((unsigned)csize);
+    lc.blockDim = dim3((unsigned)g->T);
+    lc.dynamicSmemBytes = g->smem;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    int nclusters = 0;
+    e = cudaOccupancyMaxActiveClusters(&nclusters, k_batch_cluster, &lc);
+    if (e != cudaSuccess || nclusters < 1) {
+        eng->set_err("no cluster of the requested size fits this GPU");
+        return UASTAR_BAD_INPUT;
+    }
+    g->csize = csize;
+    g->ctas = nclusters * csize;
+    return UASTAR_OK;
+}
+
 int32_t resolve_geometry(uastar_engine *eng, const uastar_batch_config *cfg, BatchGeometry *g) {
     int32_t rc = resolve_block_geometry(eng, cfg ? cfg->threads_per_instance : 0, cfg ? cfg->threads_per_heap : 0, g);
     if (rc) return rc;
-    const uint32_t cap = cfg && cfg->heap_capacity > 0 ? (uint32_t)cfg->heap_capacity : 2048;
-    g->stride16 = (uint32_t)next_pow2_u64(cap + 1);
-    g->stride16 = std::max<uint32_t>(g->stride16, (uint32_t)next_pow2_u64(std::max(g->topn_grid, g->topn_puzzle / 2) + 2));
+    g->set_capacity(cfg && cfg->heap_capacity > 0 ? (uint64_t)cfg->heap_capacity : 4095);
     g->load = cfg && cfg->load_factor > 0 && cfg->load_factor < 1 ? cfg->load_factor : 0.5;
     if (cfg && cfg->ctas > 0) g->ctas = std::min(g->ctas, cfg->ctas);
     return UASTAR_OK;
@@ -334,7 +442,7 @@ int32_t resolve_geometry(uastar_engine *eng, const uastar_batch_config *cfg, Bat
 
 // Runs `idx` (indices into insts) as one wave; fills results for them.
 int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::vector<int> &idx,
-                 const BatchGeometry &g, const std::vector<int> &space_mult, bool use_graph,
+                 const BatchGeometry &g, const std::vector<int> &space_mult, bool use_graph, uint64_t budget,
                  uastar_instance_result *results, uastar_batch_stats *stats, std::vector<int> *retry) {
     cudaError_t e;
     const int cnt = (int)idx.size();
@@ -378,7 +486,13 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
     }
     // device buffers
     const size_t tab_b = tab_slots * sizeof(Slot);
-    const size_t heap_b = (size_t)g.ctas * g.H * g.stride16 * 16;
+    const size_t heap_b = (size_t)g.ctas * g.H * g.slice;
+    if (debug_log())
+        std::fprintf(stderr, "[uastar] wave: %d instances, %s teams of %d CTAs x %d threads, %d heaps each, "
+                             "budget %llu rounds, partitions %.2f GB, heap slices %.2f GB (%llu B/heap)\n",
+                     cnt, g.csize > 0 ? "cluster" : "CTA", g.csize > 0 ? g.csize : 1, g.T, (int)g.H,
+                     (unsigned long long)budget, tab_slots * 32.0 / 1e9, heap_b / 1e9,
+                     (unsigned long long)g.slice);
     if ((e = eng->b_tab.ensure(tab_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc partitions");
     if ((e = eng->b_heaps.ensure(heap_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc heap slices");
     if ((e = eng->b_hsize.ensure((size_t)g.ctas * g.H * 4)) != cudaSuccess) return fail_cuda(eng, e, "alloc");
@@ -413,17 +527,43 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
     a.pdb4 = eng->pdb[4].as<uint8_t>();
     a.tab = eng->b_tab.as<Slot>();
     a.heaps = eng->b_heaps.as<uint8_t>();
-    a.stride16 = g.stride16;
+    a.slice = g.slice;
     a.hsize = eng->b_hsize.as<uint32_t>();
     a.cand = eng->b_cand.as<Cand>();
     a.outs = eng->b_out.as<InstOut>();
-    a.max_load = 0.9;
+    a.max_load = 0.75;
     a.budget = ~0ull;
     a.serving = 0;
     a.H = g.H;
-    a.topn_grid = g.topn_grid;
-    a.topn_puzzle = g.topn_puzzle;
-    const int ctas = std::min(g.ctas, cnt);
+    a.L_grid = g.L_grid;
+    a.L_puzzle = g.L_puzzle;
+    a.stride_grid = g.hg_grid.stride;
+    a.stride_puzzle = g.hg_puzzle.stride;
+    a.hcap_grid = g.hg_grid.hcap;
+    a.hcap_puzzle = g.hg_puzzle.hcap;
+    a.budget = budget;
+    int ctas = std::min(g.ctas, cnt);
+    cudaLaunchConfig_t lc = {};
+    cudaLaunchAttribute lat[1];
+    if (g.csize > 0) {
+        const int nclusters = std::min(g.ctas / g.csize, cnt);
+        ctas = nclusters * g.csize;
+        if ((e = eng->b_cstate.ensure((size_t)nclusters * sizeof(TeamState))) != cudaSuccess ||
+            (e = eng->b_cnext.ensure((size_t)nclusters * 4 + 64)) != cudaSuccess)
+            return fail_cuda(eng, e, "alloc cluster state");
+        a.cstates = eng->b_cstate.as<TeamState>();
+        a.cnext = eng->b_cnext.as<uint32_t>();
+        lat[0].id = cudaLaunchAttributeClusterDimension;
+        lat[0].val.clusterDim.x = (unsigned)g.csize;
+        lat[0].val.clusterDim.y = 1;
+        lat[0].val.clusterDim.z = 1;
+        lc.gridDim = dim3((unsigned)ctas);
+        lc.blockDim = dim3((unsigned)g.T);
+        lc.dynamicSmemBytes = g.smem;
+        lc.stream = eng->stream;
+        lc.attrs = lat;
+        lc.numAttrs = 1;
+    }
 
     cudaEvent_t k0, k1;
     cudaEventCreate(&k0);
@@ -432,7 +572,10 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
     cudaGraphExec_t exec = nullptr;
     auto enqueue = [&]() {
         cudaMemsetAsync(eng->b_queue.p, 0, 4, eng->stream);
-        k_batch<<<ctas, g.T, g.smem, eng->stream>>>(a);
+        if (g.csize > 0)
+            cudaLaunchKernelEx(&lc, k_batch_cluster, a);
+        else
+            k_batch<<<ctas, g.T, g.smem, eng->stream>>>(a);
     };
     cudaEventRecord(k0, eng->stream);
     if (use_graph) {
@@ -465,6 +608,14 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
     cudaEventDestroy(k0);
     cudaEventDestroy(k1);
     if (stats) stats->kernel_ms += kms;
+    if (debug_log()) {
+        int hist[16] = {0};
+        for (int p = 0; p < cnt; ++p) hist[std::min<uint32_t>(outs[p].status, 15)]++;
+        std::fprintf(stderr, "[uastar]   kernel %.1f ms; status counts:", kms);
+        for (int q = 0; q < 16; ++q)
+            if (hist[q]) std::fprintf(stderr, " %d:%d", q, hist[q]);
+        std::fprintf(stderr, "\n");
+    }
 
     // paths of solved instances: one walker thread each
     std::vector<uint32_t> which;
@@ -522,7 +673,7 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
             stats->expanded += (int64_t)o.expanded;
             stats->generated += (int64_t)o.generated;
         }
-        if ((o.status == ST_HASH_FULL || o.status == ST_HEAP_OVERFLOW) && retry) {
+        if ((o.status == ST_HASH_FULL || o.status == ST_HEAP_OVERFLOW || o.status == ST_RUNNING) && retry) {
             retry->push_back(idx[j]);
             continue;
         }
@@ -612,24 +763,46 @@ int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int
         }
         todo.push_back(i);
     }
+    // Tiers: single-CTA teams for small instances (with a round budget, so
+    // that an unexpectedly large one moves on instead of holding a CTA),
+    // cluster teams of 8 CTAs for large grids, for instances that ran out of
+    // rounds and for those that overflowed (with 16x the space); whatever
+    // overflows a cluster team goes to the plain engine (the whole GPU).
     std::vector<int> mult(count, 1);
-    BatchGeometry gw = g;
     const bool use_graph = !cfg || cfg->use_graph != 0 || cfg->threads_per_instance == 0;
-    // Waves of CTA teams; an instance that overflowed twice is a large one and
-    // is escalated to the plain engine (the whole GPU as its team, tables
-    // grown in place of a third wave).
-    for (int wave = 0; wave < 2 && !todo.empty(); ++wave) {
-        std::vector<int> retry, m(todo.size());
-        for (size_t j = 0; j < todo.size(); ++j) m[j] = mult[todo[j]];
-        rc = run_wave(eng, insts, todo, gw, m, use_graph, results, stats, &retry);
+    const uint64_t big_cells = 2048ull * 2048ull;
+    std::vector<int> tier1, tier2, retry;
+    for (int i : todo) {
+        const uastar_instance &in = insts[i];
+        if (in.kind == UASTAR_KIND_GRID && (uint64_t)in.H * in.W > big_cells)
+            tier2.push_back(i);
+        else
+            tier1.push_back(i);
+    }
+    if (!tier1.empty()) {
+        std::vector<int> m(tier1.size(), 1);
+        rc = run_wave(eng, insts, tier1, g, m, use_graph, 4096, results, stats, &retry);
         if (rc) return rc;
-        for (int i : retry) mult[i] *= 8;
+        // running out of rounds proves an instance large just as an overflow does
+        for (int i : retry) {
+            mult[i] = 16;
+            tier2.push_back(i);
+        }
+    }
+    todo.clear();
+    if (!tier2.empty()) {
+        BatchGeometry gc = g;
         bool heap_over = false;
-        for (int i : retry) heap_over |= results[i].status == UASTAR_HEAP_OVERFLOW;
-        if (heap_over) gw.stride16 *= 4;
-        // a retry wave runs fewer instances: fewer CTAs keep the heap slices small
-        gw.ctas = std::min<int>(g.ctas, std::max<int>(1, (int)retry.size()));
-        todo.swap(retry);
+        for (int i : tier2) heap_over |= results[i].status == UASTAR_HEAP_OVERFLOW;
+        if (heap_over) gc.set_capacity(g.want * 16 + 15);
+        rc = resolve_cluster_geometry(eng, 8, &gc);
+        if (rc) return rc;
+        std::vector<int> m(tier2.size());
+        for (size_t j = 0; j < tier2.size(); ++j) m[j] = mult[tier2[j]] * 2;
+        retry.clear();
+        rc = run_wave(eng, insts, tier2, gc, m, use_graph, ~0ull, results, stats, &retry);
+        if (rc) return rc;
+        todo = retry;
     }
     // the partitions of a large batch can hold a large share of HBM: return them
     eng->b_tab.release();
@@ -638,6 +811,7 @@ int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int
         const uastar_instance &in = insts[i];
         uastar_instance_result &r = results[i];
         r.attempts += 1;
+        const double te = now_ms();
         if (in.kind == UASTAR_KIND_GRID) {
             uastar_grid_result gr;
             rc = uastar_grid_solve(eng, in.words, in.H, in.W, in.sx, in.sy, in.ex, in.ey, &gr);
@@ -666,12 +840,15 @@ int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int
             }
         }
         if (stats) stats->escalated += 1;
+        if (debug_log())
+            std::fprintf(stderr, "[uastar] escalated instance %d (%s) to the plain engine: status %d, %.1f ms\n", i,
+                         in.kind == UASTAR_KIND_GRID ? "grid" : "puzzle", r.status, now_ms() - te);
     }
     if (stats) {
         stats->wall_ms = now_ms() - t0;
         stats->ctas = g.ctas;
         stats->threads_per_instance = g.T;
-        stats->heap_capacity = (int32_t)g.stride16 - 1;
+        stats->heap_capacity = (int32_t)g.hg_puzzle.hcap;
         stats->load_factor = g.load;
     }
     for (int i = 0; i < count; ++i) results[i].latency_ms = now_ms() - t0;
@@ -792,7 +969,6 @@ struct ServeState {
     uastar_serve_config cfg{};
     int T = 256, S = 0;
     BatchGeometry geo{};
-    uint32_t stride16 = 2048;
     uint64_t heap_bytes = 0;
     std::thread th;
     std::mutex mu;
@@ -889,19 +1065,24 @@ static void serve_loop(ServeState *S) {
             if (free_slot >= S->S) break;
             const uint64_t tn = serve_partition_slots(S, r);
             const uint64_t bn = r.inst.kind == UASTAR_KIND_GRID ? r.words.size() + 2 : 0;
-            const uint32_t hstride = S->stride16 * r.heap_mult;
-            const uint64_t hn = (uint64_t)S->geo.H * hstride;
+            // heap slice: H heaps of the request's entry type, grown 8x per overflow
+            BatchGeometry hgeo = S->geo;
+            hgeo.set_capacity((S->geo.want + 1) * r.heap_mult - 1);
+            const bool grid = r.inst.kind == UASTAR_KIND_GRID;
+            const uint32_t hstride = grid ? hgeo.hg_grid.stride : hgeo.hg_puzzle.stride;
+            const uint32_t hhcap = grid ? hgeo.hg_grid.hcap : hgeo.hg_puzzle.hcap;
+            const uint64_t hn = ((uint64_t)S->geo.H * hstride * (grid ? 16 : 8) + 127) / 128 * 8;  // 16-byte units
             if (tn > S->tab_alloc.capacity() || bn > S->bm_alloc.capacity() || hn > S->heap_alloc.capacity()) {
                 serve_complete(S, r, UASTAR_REJECTED);  // can never fit the budget
                 continue;
             }
             uint64_t toff = 0, boff = 0, hoff = 0;
-            if (!S->tab_alloc.alloc(tn, 1, &toff)) break;  // wait for memory to free up
+            if (!S->tab_alloc.alloc(tn, 4, &toff)) break;  // wait for memory to free up
             if (bn && !S->bm_alloc.alloc(bn, 2, &boff)) {
                 S->tab_alloc.release(toff, tn);
                 break;
             }
-            if (!S->heap_alloc.alloc(hn, 2, &hoff)) {
+            if (!S->heap_alloc.alloc(hn, 8, &hoff)) {
                 S->tab_alloc.release(toff, tn);
                 if (bn) S->bm_alloc.release(boff, bn);
                 break;
@@ -923,9 +1104,14 @@ static void serve_loop(ServeState *S) {
             d.max_rounds = eng->cfg.max_rounds;
             d.tab_off = toff;
             d.log2_slots = (uint32_t)log2_u64(tn);
-            d.fresh = 1;
-            d.heap_off16 = hoff;
-            d.heap_stride16 = hstride;
+            d.fresh = 2;
+            if (fill_ff_async(eng, S->tab.as<Slot>() + toff, tn * sizeof(Slot), S->stream) != UASTAR_OK) {
+                S->loop_error = UASTAR_CUDA_ERROR;
+                break;
+            }
+            d.heap_off = hoff * 16;
+            d.heap_stride = hstride;
+            d.heap_hcap = hhcap;
             if (d.kind == UASTAR_KIND_GRID) {
                 d.H = sl.req.inst.H;
                 d.W = sl.req.inst.W;
@@ -975,15 +1161,14 @@ static void serve_loop(ServeState *S) {
         a.pdb4 = eng->pdb[4].as<uint8_t>();
         a.tab = S->tab.as<Slot>();
         a.heaps = S->heaps.as<uint8_t>();
-        a.stride16 = S->stride16;
         a.hsize = S->hsize.as<uint32_t>();
         a.cand = S->cand.as<Cand>();
         a.outs = S->outs.as<InstOut>();
         a.states = S->states.as<TeamState>();
-        a.max_load = 0.9;
+        a.max_load = 0.75;
         a.H = S->geo.H;
-        a.topn_grid = S->geo.topn_grid;
-        a.topn_puzzle = S->geo.topn_puzzle;
+        a.L_grid = S->geo.L_grid;
+        a.L_puzzle = S->geo.L_puzzle;
         a.budget = (uint64_t)(S->cfg.rounds_per_quantum > 0 ? S->cfg.rounds_per_quantum : 256);
         a.serving = 1;
         cudaEventRecord(S->q0, S->stream);
@@ -1065,7 +1250,7 @@ static void serve_loop(ServeState *S) {
             if ((status == ST_HASH_FULL || status == ST_HEAP_OVERFLOW) && r.attempts < 10) {
                 // re-queue with 4x the space, ahead of later arrivals
                 if (status == ST_HASH_FULL) r.mult *= 4;
-                else r.heap_mult *= 4;
+                else r.heap_mult *= 16;
                 pending.insert(pending.begin(), std::move(r));
                 sl = ServeSlotState();
                 continue;
@@ -1150,9 +1335,7 @@ int32_t uastar_serve_start(uastar_engine *eng, const uastar_serve_config *cfg) {
         return grc;
     }
     S->T = S->geo.T;
-    S->stride16 = (uint32_t)next_pow2_u64((uint64_t)(S->cfg.heap_capacity > 0 ? S->cfg.heap_capacity : 2048) + 1);
-    S->stride16 = std::max<uint32_t>(
-        S->stride16, (uint32_t)next_pow2_u64(std::max(S->geo.topn_grid, S->geo.topn_puzzle / 2) + 2));
+    S->geo.set_capacity(S->cfg.heap_capacity > 0 ? (uint64_t)S->cfg.heap_capacity : 4095);
     const int max_slots = S->geo.ctas;
     cudaError_t e = cudaSuccess;
     S->S = S->cfg.slots > 0 ? std::min(S->cfg.slots, max_slots) : max_slots;
@@ -1163,7 +1346,7 @@ int32_t uastar_serve_start(uastar_engine *eng, const uastar_serve_config *cfg) {
     const uint64_t bm_words = (uint64_t)(budget_b * 0.05 / 8);
     const double tab_b = budget_b * 0.75;
     S->heap_bytes = heap_entries * 16;
-    if (tab_b < (double)(1u << 20) * sizeof(Slot) || heap_entries < (uint64_t)S->geo.H * S->stride16) {
+    if (tab_b < (double)(1u << 20) * sizeof(Slot) || heap_entries * 16 < (uint64_t)S->geo.H * S->geo.slice) {
         delete S;
         eng->set_err("serving budget too small");
         return UASTAR_BAD_INPUT;

@@ -29,11 +29,10 @@ __global__ void k_fill_ff(uint4 *p, size_t n16) {
 
 template <class P>
 __global__ void __launch_bounds__(512, 1) k_plain_search(P prob, SearchMem<typename P::Entry> m,
-                                                      TeamState *st, uint64_t timeout_ns, uint32_t H,
-                                                      uint32_t topn) {
-    extern __shared__ __align__(16) unsigned char smem[];
+                                                      TeamState *st, uint64_t timeout_ns, uint32_t H) {
+    extern __shared__ __align__(128) unsigned char smem[];
     GridTeam team{st, 0u, timeout_ns};
-    ga_search<P>(prob, team, m, H, topn, smem, ~0ull);
+    ga_search<P>(prob, team, m, H, smem, ~0ull);
 }
 
 // Walk the prev chain from the goal slot (one thread: a pointer chase).
@@ -48,6 +47,15 @@ __global__ void k_walk(const Slot *tab, uint32_t goal_slot, unsigned long long *
         s = __ldcg(&tab[s].prev);
     }
     *len = (s != kNone) ? cap + 1 : n;
+}
+
+int32_t fill_ff_async(uastar_engine *eng, void *p, size_t bytes, cudaStream_t stream) {
+    const size_t n16 = bytes / 16;
+    const int blocks = (int)std::min<size_t>((n16 + 255) / 256, (size_t)std::max(1, eng->sms * 8));
+    k_fill_ff<<<std::max(1, blocks), 256, 0, stream>>>(static_cast<uint4 *>(p), n16);
+    eng->launches++;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? UASTAR_OK : fail_cuda(eng, e, "fill");
 }
 
 int32_t fail_cuda(uastar_engine *eng, cudaError_t e, const char *what) {
@@ -102,16 +110,15 @@ struct PlainOut {
 
 // Run one instance with the whole GPU as the team.  Grows the dedup table /
 // heaps and retries when they overflow and were auto-sized.
-// Shared-memory heap levels that fit: the largest L with H * 2^L entries
-// (plus the pop records) under `budget` bytes.
-template <class P> uint32_t fit_topn(uint32_t H, int levels, size_t budget) {
-    if (levels < 0) return 0;
-    uint32_t best = 0;
-    for (int L = 1; L <= 12; ++L) {
-        const uint32_t topn = (1u << L) - 1;
-        if (SearchSmem<P>::bytes(H, topn) > budget) break;
-        best = topn;
-        if (levels > 0 && L == levels) break;
+// Shared-memory heap levels: the largest L (at least 1) whose tops, pop
+// records and brick scratch fit `budget` bytes, or exactly `levels` if > 0.
+template <class P> uint32_t fit_levels(uint32_t H, int levels, size_t budget) {
+    if (levels > 0) return (uint32_t)std::min(levels, 12);
+    uint32_t best = 1;
+    if (levels < 0) return best;
+    for (uint32_t L = 1; L <= 12; ++L) {
+        if (SearchSmem<P>::bytes(H, L) > budget) break;
+        best = L;
     }
     return best;
 }
@@ -136,8 +143,8 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, eng->device);
     const int per_sm = (int)((nblocks + eng->sms - 1) / eng->sms);
     const size_t smem_budget = (size_t)std::max(8 * 1024, std::min(smem_optin, smem_sm / std::max(1, per_sm) - 2048));
-    const uint32_t topn = fit_topn<P>(H, c.heap_top_levels, smem_budget);
-    const size_t smem = SearchSmem<P>::bytes(H, topn);
+    const uint32_t L = fit_levels<P>(H, c.heap_top_levels, smem_budget);
+    const size_t smem = SearchSmem<P>::bytes(H, L);
     cudaError_t e = cudaFuncSetAttribute(k_plain_search<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return fail_cuda(eng, e, "smem attribute");
     int max_active = 0;
@@ -147,12 +154,12 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
         eng->set_err("heaps / (block_threads / threads_per_heap) exceed one co-resident wave of the GPU");
         return UASTAR_BAD_INPUT;
     }
-    if (stride <= topn + 1) stride = next_pow2_u32(topn + 2);
+    HeapGeometry<P> hg = heap_geometry<P>(L, stride);
 
     for (int attempt = 0; attempt < 6; ++attempt) {
         const uint64_t slots = 1ull << log2;
         const size_t tab_b = slots * sizeof(Slot);
-        const size_t heap_b = (size_t)k * stride * sizeof(E);
+        const size_t heap_b = (size_t)k * hg.stride * sizeof(E);
         const size_t cand_b = (size_t)k * P::kMoves * sizeof(Cand);
         if ((e = eng->tab.ensure(tab_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc table");
         if ((e = eng->heaps.ensure(heap_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc heaps");
@@ -175,15 +182,17 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
         m.max_inserted = (uint64_t)((double)slots * c.max_load);
         m.max_probe = 4096;
         m.heaps = eng->heaps.as<E>();
-        m.stride = stride;
+        m.stride = hg.stride;
+        m.hcap = hg.hcap;
+        m.L = L;
         m.heap_size = eng->heap_size.as<uint32_t>();
         m.cand = eng->cand.as<Cand>();
         m.max_rounds = (uint64_t)c.max_rounds;
         TeamState *st = eng->team.as<TeamState>();
         uint64_t timeout_ns = (uint64_t)(c.wait_timeout_s * 1e9);
         P pr = prob;
-        uint32_t h_arg = H, topn_arg = topn;
-        void *args[] = {&pr, &m, &st, &timeout_ns, &h_arg, &topn_arg};
+        uint32_t h_arg = H;
+        void *args[] = {&pr, &m, &st, &timeout_ns, &h_arg};
         cudaEventRecord(eng->ev0, eng->stream);
         e = cudaLaunchCooperativeKernel((const void *)k_plain_search<P>, dim3(nblocks), dim3(block),
                                         args, smem, eng->stream);
@@ -207,9 +216,9 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
             log2 += 2;
             continue;
         }
-        if (s == ST_HEAP_OVERFLOW && c.heap_capacity <= 0 && stride < (1u << 18) &&
-            (size_t)k * stride * 4 * sizeof(E) < free_b + eng->heaps.bytes) {
-            stride *= 4;
+        if (s == ST_HEAP_OVERFLOW && c.heap_capacity <= 0 && hg.hcap < (1u << 22) &&
+            (size_t)k * hg.stride * 8 * sizeof(E) < free_b + eng->heaps.bytes) {
+            hg = heap_geometry<P>(L, (uint64_t)hg.hcap * 8);
             continue;
         }
         break;
@@ -399,7 +408,7 @@ uastar_engine *uastar_create(int32_t ordinal, const uastar_config *cfg) {
     if (c.heaps <= 0) c.heaps = 8192;
     if (c.block_threads <= 0) c.block_threads = 256;
     c.block_threads = std::max(32, std::min(512, (c.block_threads + 31) / 32 * 32));
-    if (!(c.max_load > 0.0 && c.max_load < 1.0)) c.max_load = 0.9;
+    if (!(c.max_load > 0.0 && c.max_load < 1.0)) c.max_load = 0.8;
     if (c.max_rounds <= 0) c.max_rounds = 1ll << 31;
     if (!(c.wait_timeout_s > 0.0)) c.wait_timeout_s = 10.0;
     cudaError_t e = cudaSetDevice(ordinal);
@@ -423,7 +432,7 @@ void uastar_destroy(uastar_engine *eng) {
     for (DevBuf *b : {&eng->tab, &eng->heaps, &eng->heap_size, &eng->cand, &eng->team, &eng->walk,
                       &eng->bitmap, &eng->b_desc, &eng->b_out, &eng->b_queue, &eng->b_bitmaps,
                       &eng->b_tab, &eng->b_heaps, &eng->b_hsize, &eng->b_cand, &eng->b_walk,
-                      &eng->b_walklen})
+                      &eng->b_walklen, &eng->b_cstate, &eng->b_cnext})
         b->release();
     for (auto &b : eng->pdb) b.release();
     if (eng->ev0) cudaEventDestroy(eng->ev0);

@@ -74,7 +74,7 @@ struct uastar_engine {
 
     // batched / serving engines
     uastar::DevBuf b_desc, b_out, b_queue, b_bitmaps, b_tab, b_heaps, b_hsize, b_cand, b_walk,
-        b_walklen;
+        b_walklen, b_cstate, b_cnext;
     uastar::ServeState *serve = nullptr;  // owned; released by uastar_serve_stop
 
     void set_err(const std::string &s) { err = s; }
@@ -83,6 +83,8 @@ struct uastar_engine {
 namespace uastar {
 // engine.cu
 int32_t fail_cuda(uastar_engine *eng, cudaError_t e, const char *what);
+// Fill `bytes` (a multiple of 16) at `p` with 0xFF on `stream` using the whole GPU.
+int32_t fill_ff_async(uastar_engine *eng, void *p, size_t bytes, cudaStream_t stream);
 // pdb.cu
 int32_t pdb_build_device(uastar_engine *eng, int n, double *ms);
 }  // namespace uastar

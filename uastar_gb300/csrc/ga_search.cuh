@@ -47,8 +47,10 @@ template <class E> struct SearchMem {
     uint64_t mask;          // slots - 1 (power of two)
     uint64_t max_inserted;  // load limit
     uint32_t max_probe;
-    E *heaps;               // k heaps of `stride` entries (index 0 unused), CTA c owns [c*H, (c+1)*H)
-    uint32_t stride;
+    E *heaps;               // k heaps of `stride` entries, CTA c owns heaps [c*H, (c+1)*H)
+    uint32_t stride;        // entries per heap: saved shared top, then the bricks
+    uint32_t hcap;          // maximum heap size
+    uint32_t L;             // heap levels kept in shared memory (>= 1)
     uint32_t *heap_size;    // k sizes
     Cand *cand;             // >= k * kMoves records
     uint64_t max_rounds;    // absolute round limit (ITER_LIMIT)
@@ -62,6 +64,30 @@ struct GridTeam {
     __device__ uint32_t cta() const { return blockIdx.x; }
     __device__ uint32_t ctas() const { return gridDim.x; }
     __device__ void sync() { grid_barrier(&st->barrier, gridDim.x, epoch, &st->error, timeout_ns); }
+    __device__ uint64_t rd64(const unsigned long long *p) const { return ldcg_u64(p); }
+    __device__ uint32_t rd32(const uint32_t *p) const { return ldcg_u32(p); }
+};
+
+// A thread-block cluster as one team: CTA rank within the cluster, hardware
+// cluster barrier (barrier.cluster arrive.release / wait.acquire; all CTAs of
+// a cluster are co-scheduled, so the barrier needs no time bound), team
+// state in global memory read through L2.
+struct ClusterTeam {
+    TeamState *st;  // global memory
+    __device__ uint32_t cta() const {
+        uint32_t r;
+        asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+        return r;
+    }
+    __device__ uint32_t ctas() const {
+        uint32_t r;
+        asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+        return r;
+    }
+    __device__ void sync() {
+        __threadfence();
+        asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+    }
     __device__ uint64_t rd64(const unsigned long long *p) const { return ldcg_u64(p); }
     __device__ uint32_t rd32(const uint32_t *p) const { return ldcg_u32(p); }
 };
@@ -80,53 +106,128 @@ struct BlockTeam {
 };
 
 // ------------------------------------------------------------------ heaps ---
-// A 1-indexed binary heap whose entries 1..topn live in shared memory and the
-// rest in global memory (the global array keeps the same indices).  The two
-// children 2i, 2i+1 of a node are adjacent.
-template <class P> struct HeapRef {
+// A 1-indexed binary min-heap.  Entries 1..2^L-1 (the top L levels) live in
+// shared memory.  Below them the tree is cut into bricks: complete subtrees
+// of D levels whose 2^D - 1 entries fill one 128-byte line in global memory
+// (D = 3 for 16-byte entries, 4 for 8-byte entries; slot 0 of a brick is
+// unused).  A sift-down reads both child bricks of a node in one burst of
+// independent loads, so it waits on global memory once per D levels instead
+// of once per level.  Bricks are stored level by level: the 2^(L + b*D)
+// bricks of brick level b follow the 2^L (2^(b*D) - 1) / (2^D - 1) bricks of
+// the levels above it, in the order of their root indices.
+template <class P> struct BrickHeap {
     using E = typename P::Entry;
-    E *g;          // global array, index 0 unused
-    E *s;          // shared top, index 0 unused
-    uint32_t topn; // entries held in shared memory
-    __device__ __forceinline__ E ld(uint32_t i) const { return i <= topn ? s[i] : P::load(g + i); }
+    static constexpr uint32_t D = sizeof(E) == 16 ? 3 : 4;
+    static constexpr uint32_t BE = 1u << D;  // entries per brick line
+    static_assert(BE * sizeof(E) == 128, "one brick per 128-byte line");
+    E *g;       // this heap's bricks
+    E *s;       // shared top, index 0 unused
+    E *scr;     // shared scratch: two bricks
+    uint32_t L; // levels in shared memory
+
+    __device__ __forceinline__ uint32_t topn() const { return (1u << L) - 1; }
+    // global entry offset of heap index i (i > topn)
+    __device__ __forceinline__ uint64_t off(uint32_t i) const {
+        const uint32_t l = 31u - (uint32_t)__clz(i);
+        const uint32_t r = l - L;
+        const uint32_t bl = r / D;
+        const uint32_t d = r - bl * D;
+        const uint32_t root = i >> d;
+        const uint32_t local = (1u << d) | (i & ((1u << d) - 1u));
+        const uint64_t first = (((1ull << (bl * D)) - 1ull) << L) / (BE - 1u);
+        const uint64_t id = first + (root - (1ull << (L + bl * D)));
+        return id * BE + local;
+    }
+    __device__ __forceinline__ E ld(uint32_t i) const { return i <= topn() ? s[i] : P::load(g + off(i)); }
     __device__ __forceinline__ void st(uint32_t i, const E &v) const {
-        if (i <= topn)
+        if (i <= topn())
             s[i] = v;
         else
-            P::store(g + i, v);
+            P::store(g + off(i), v);
+    }
+    // Copy the brick rooted at heap index `root` into scratch half `h`.
+    __device__ __forceinline__ void fetch(uint32_t root, uint32_t h) const {
+        const uint4 *src = reinterpret_cast<const uint4 *>(g + off(root) - 1);
+        uint4 *dst = reinterpret_cast<uint4 *>(scr + h * BE);
+        uint4 v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = __ldcg(src + q);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) dst[q] = v[q];
     }
 };
 
+// Remove the root: returns it in `out`; `last` (the old heap[size]) is sifted
+// down from the root hole.  `size` is the size after removal.
 template <class P>
-__device__ __forceinline__ bool heap_pop(const HeapRef<P> &h, uint32_t &size, typename P::Entry &out) {
+__device__ __forceinline__ void heap_sift_down(const BrickHeap<P> &h, uint32_t size, typename P::Entry last) {
     using E = typename P::Entry;
-    if (size == 0) return false;
-    out = h.ld(1);
-    const E last = h.ld(size);
-    size -= 1;
-    if (size == 0) return true;
+    constexpr uint32_t D = BrickHeap<P>::D, BE = BrickHeap<P>::BE;
+    const uint32_t topn = h.topn();
     uint32_t now = 1;
+    // shared-memory levels
     for (;;) {
         uint32_t c = now << 1;
-        if (c > size) break;
-        E a = h.ld(c);
+        if (c > size || c > topn) break;
+        E a = h.s[c];
         if (c < size) {
-            const E b = h.ld(c + 1);
+            const E b = h.s[c + 1];
             if (P::less(b, a)) {
                 a = b;
                 ++c;
             }
         }
-        if (!P::less(a, last)) break;
-        h.st(now, a);
+        if (!P::less(a, last)) {
+            h.s[now] = last;
+            return;
+        }
+        h.s[now] = a;
         now = c;
     }
+    if ((now << 1) > size) {
+        h.st(now, last);
+        return;
+    }
+    // global bricks: `half` is the scratch half holding the brick of `now`
+    // (none while `now` is in shared memory), `depth` its level in that brick
+    int half = -1;
+    uint32_t depth = 0;
+    for (;;) {
+        uint32_t c = now << 1;
+        if (c > size) break;
+        E a, b;
+        const bool two = c < size;
+        int ch = half;
+        if (half >= 0 && depth + 1 < D) {
+            const uint32_t la = (1u << (depth + 1)) | (c & ((1u << (depth + 1)) - 1u));
+            a = h.scr[half * BE + la];
+            if (two) b = h.scr[half * BE + la + 1];
+        } else {
+            // the children are the roots of two bricks
+            h.fetch(c, 0);
+            if (two) h.fetch(c + 1, 1);
+            a = h.scr[1];
+            if (two) b = h.scr[BE + 1];
+            ch = 0;
+        }
+        bool right = two && P::less(b, a);
+        if (right) a = b;
+        if (!P::less(a, last)) break;
+        h.st(now, a);
+        if (half >= 0 && depth + 1 < D) {
+            depth += 1;
+        } else {
+            half = right ? 1 : 0;
+            depth = 0;
+            (void)ch;
+        }
+        now = c + (right ? 1u : 0u);
+    }
     h.st(now, last);
-    return true;
 }
 
 template <class P>
-__device__ __forceinline__ void heap_push(const HeapRef<P> &h, uint32_t &size, const typename P::Entry &v) {
+__device__ __forceinline__ void heap_push(const BrickHeap<P> &h, uint32_t &size, const typename P::Entry &v) {
     using E = typename P::Entry;
     uint32_t now = ++size;
     while (now > 1) {
@@ -137,6 +238,31 @@ __device__ __forceinline__ void heap_push(const HeapRef<P> &h, uint32_t &size, c
         now = par;
     }
     h.st(now, v);
+}
+
+// Global entries per heap and the largest heap size for L shared levels and
+// a requested capacity (host side).
+template <class P> struct HeapGeometry {
+    uint32_t stride;  // entries of global memory per heap (saved top + bricks)
+    uint32_t hcap;    // maximum heap size
+};
+// Offset of the bricks within a heap's global block: the first entries hold
+// the shared top while a resumable search is parked.
+template <class P> __host__ __device__ constexpr uint32_t top_reserve(uint32_t L) {
+    return ((1u << L) + BrickHeap<P>::BE - 1u) / BrickHeap<P>::BE * BrickHeap<P>::BE;
+}
+template <class P> __host__ HeapGeometry<P> heap_geometry(uint32_t L, uint64_t want) {
+    constexpr uint32_t D = BrickHeap<P>::D, BE = BrickHeap<P>::BE;
+    uint32_t levels = 0;
+    while (levels < 30 && ((1ull << levels) - 1) < want) ++levels;
+    uint32_t nbl = levels > L ? (levels - L + D - 1) / D : 1;
+    if (nbl < 1) nbl = 1;
+    while (L + nbl * D > 31) --nbl;
+    const uint64_t bricks = (((1ull << (nbl * D)) - 1ull) << L) / (BE - 1u);
+    HeapGeometry<P> geo;
+    geo.stride = (uint32_t)(bricks * BE) + top_reserve<P>(L);
+    geo.hcap = (uint32_t)((1ull << (L + nbl * D)) - 1ull);
+    return geo;
 }
 
 // ---------------------------------------------------------- cost minima ---
@@ -180,41 +306,56 @@ enum : int { RELAX_NONE = 0, RELAX_IMPROVED = 1, RELAX_INSERTED = 3, RELAX_FULL 
 // RELAX_IMPROVED (existing slot, g strictly lowered), RELAX_NONE (existing
 // slot, g not better) or RELAX_FULL (probe limit).
 template <class P>
+__device__ __forceinline__ int relax_at(Slot *tab, uint64_t h, KeyG cur, uint64_t key, uint64_t g,
+                                        uint32_t *slot_out) {
+    // cur.key == key: lower g; the key half never changes once set
+    *slot_out = (uint32_t)h;
+    while (P::cost_cmp(g, cur.g) < 0) {
+        const KeyG old = cas128(tab + h, cur, KeyG{key, g});
+        if (old.key == cur.key && old.g == cur.g) return RELAX_IMPROVED;
+        cur = old;
+    }
+    return RELAX_NONE;
+}
+
+template <class P>
 __device__ __forceinline__ int relax(Slot *tab, uint64_t mask, uint32_t max_probe, uint64_t key, uint64_t g,
                                      uint32_t *slot_out) {
+    // Linear probing.  The home slot is tried with one 16-byte CAS; past it
+    // the probe reads the rest of the home slot's 128-byte line (4 slots) and
+    // then whole lines, one dependent load per line.
     uint64_t h = mix64(key) & mask;
     const KeyG empty{kEmptyKey, kInfCost};
-    for (uint32_t i = 0; i < max_probe; ++i) {
-        KeyG cur;
-        if (i == 0) {
-            cur = cas128(tab + h, empty, KeyG{key, g});
-            if (cur.key == kEmptyKey) {
-                *slot_out = (uint32_t)h;
-                return RELAX_INSERTED;
-            }
-        } else {
-            const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(tab + h));
-            cur.key = v.x;
-            cur.g = v.y;
-            if (cur.key == kEmptyKey) {
-                cur = cas128(tab + h, empty, KeyG{key, g});
+    KeyG cur = cas128(tab + h, empty, KeyG{key, g});
+    if (cur.key == kEmptyKey) {
+        *slot_out = (uint32_t)h;
+        return RELAX_INSERTED;
+    }
+    if (cur.key == key) return relax_at<P>(tab, h, cur, key, g, slot_out);
+    uint32_t probed = 1;
+    h = (h + 1) & mask;
+    while (probed < max_probe) {
+        // slots h .. end of h's line (the table is line-aligned, mask >= 3)
+        const uint32_t n = 4u - (uint32_t)(h & 3u);
+        ulonglong2 v[4];
+#pragma unroll
+        for (uint32_t q = 0; q < 4; ++q)
+            if (q < n) v[q] = __ldcg(reinterpret_cast<const ulonglong2 *>(tab + h + q));
+        for (uint32_t q = 0; q < n; ++q) {
+            const uint64_t hq = h + q;
+            if (v[q].x == key) return relax_at<P>(tab, hq, KeyG{v[q].x, v[q].y}, key, g, slot_out);
+            if (v[q].x == kEmptyKey) {
+                cur = cas128(tab + hq, empty, KeyG{key, g});
                 if (cur.key == kEmptyKey) {
-                    *slot_out = (uint32_t)h;
+                    *slot_out = (uint32_t)hq;
                     return RELAX_INSERTED;
                 }
+                if (cur.key == key) return relax_at<P>(tab, hq, cur, key, g, slot_out);
+                // another key took it: keep probing
             }
         }
-        if (cur.key == key) {
-            *slot_out = (uint32_t)h;
-            // lower g; the key half never changes once set
-            while (P::cost_cmp(g, cur.g) < 0) {
-                const KeyG old = cas128(tab + h, cur, KeyG{key, g});
-                if (old.key == cur.key && old.g == cur.g) return RELAX_IMPROVED;
-                cur = old;
-            }
-            return RELAX_NONE;
-        }
-        h = (h + 1) & mask;
+        probed += n;
+        h = (h + n) & mask;
     }
     return RELAX_FULL;
 }
@@ -239,12 +380,17 @@ struct PopInfo {
 };
 
 template <class P> struct SearchSmem {
-    // pops, heap tops, then a small scratch area (warp totals)
-    static __host__ __device__ size_t scratch_offset(uint32_t H, uint32_t topn) {
-        return ((size_t)H * sizeof(PopInfo) + (size_t)H * (topn + 1) * sizeof(typename P::Entry) + 15) & ~(size_t)15;
+    using E = typename P::Entry;
+    // pops, heap tops, brick scratch, then warp totals
+    static __host__ __device__ size_t tops_offset(uint32_t H) { return (size_t)H * sizeof(PopInfo); }
+    static __host__ __device__ size_t scr_offset(uint32_t H, uint32_t L) {
+        return (tops_offset(H) + (size_t)H * (1u << L) * sizeof(E) + 127) & ~(size_t)127;
     }
-    static __host__ __device__ size_t bytes(uint32_t H, uint32_t topn) {
-        return scratch_offset(H, topn) + 4 * (2 + (H + 31) / 32);
+    static __host__ __device__ size_t scratch_offset(uint32_t H, uint32_t L) {
+        return scr_offset(H, L) + (size_t)H * 2 * 128;
+    }
+    static __host__ __device__ size_t bytes(uint32_t H, uint32_t L) {
+        return scratch_offset(H, L) + 4 * (2 + (H + 31) / 32);
     }
 };
 
@@ -252,27 +398,40 @@ template <class P> struct SearchSmem {
 // Runs up to `budget` rounds (resumable: state lives in TeamState, the heaps
 // and the table).  Returns ST_RUNNING if the budget ran out first, else the
 // final status.  Every thread of every CTA of the team must call it with the
-// same H (heaps per CTA, 1 <= H <= blockDim.x) and topn; `smem` points at
-// SearchSmem<P>::bytes(H, topn) bytes of shared memory.
+// same H (heaps per CTA, 1 <= H <= blockDim.x); `smem` points at
+// SearchSmem<P>::bytes(H, m.L) bytes of shared memory (128-byte aligned).
 template <class P, class Team>
 __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typename P::Entry> &m, uint32_t H,
-                              uint32_t topn, unsigned char *smem, uint64_t budget) {
+                              unsigned char *smem, uint64_t budget) {
     using E = typename P::Entry;
     TeamState *st = team.st;
     const uint32_t T = blockDim.x, tid = threadIdx.x, lane = tid & 31u;
     const uint32_t C = team.ctas(), cta = team.cta();
     const bool owner = tid < H;
     const uint32_t myh = cta * H + tid;  // global heap index (valid when owner)
+    const uint32_t L = m.L, topn = (1u << L) - 1;
+    const uint32_t owner_warps = (H + 31u) / 32u;
+    // Warps past the owners relax successors while the owners refill their
+    // heaps' root holes; with no such warps, everyone relaxes first.
+    const uint32_t rfirst = T > owner_warps * 32u ? owner_warps * 32u : 0u;
+    const uint32_t rthreads = T - rfirst;
+    const bool relaxer = tid >= rfirst;
 
     PopInfo *pop = reinterpret_cast<PopInfo *>(smem);
-    E *tops = reinterpret_cast<E *>(smem + (size_t)H * sizeof(PopInfo));
-    uint32_t *scratch = reinterpret_cast<uint32_t *>(smem + SearchSmem<P>::scratch_offset(H, topn));
+    E *tops = reinterpret_cast<E *>(smem + SearchSmem<P>::tops_offset(H));
+    E *scr = reinterpret_cast<E *>(smem + SearchSmem<P>::scr_offset(H, L));
+    uint32_t *scratch = reinterpret_cast<uint32_t *>(smem + SearchSmem<P>::scratch_offset(H, L));
 
-    HeapRef<P> myheap{m.heaps + (size_t)(owner ? myh : 0) * m.stride, tops + (size_t)(owner ? tid : 0) * (topn + 1),
-                      topn};
+    E *const gblock = m.heaps + (size_t)(owner ? myh : 0) * m.stride;  // saved top, then bricks
+    BrickHeap<P> myheap{gblock + top_reserve<P>(L), tops + (size_t)(owner ? tid : 0) * (1u << L),
+                        scr + (size_t)(owner ? tid : 0) * 2 * BrickHeap<P>::BE, L};
     uint64_t nE = 0, nS = 0, nP = 0;
 
-    if (team.rd32(&st->started) == 0) {
+    // Every thread reads `started` before the team's rank 0 may set it below,
+    // so that all take the same branch (and the same number of barriers).
+    const bool fresh = team.rd32(&st->started) == 0;
+    team.sync();
+    if (fresh) {
         if (cta == 0 && tid == 0) {
             const uint64_t key0 = prob.start_key();
             const uint32_t aux0 = prob.start_aux();
@@ -293,7 +452,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
     } else if (owner) {
         // resuming: bring the shared top of this heap back from global memory
         const uint32_t sz = ldcg_u32(&m.heap_size[myh]);
-        for (uint32_t i = 1; i <= topn && i <= sz; ++i) myheap.s[i] = P::load(myheap.g + i);
+        for (uint32_t i = 1; i <= topn && i <= sz; ++i) myheap.s[i] = P::load(gblock + i);
     }
     __syncthreads();
 
@@ -301,16 +460,25 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
     uint64_t round = team.rd64(&st->round);
     uint32_t status = ST_RUNNING;
     uint32_t hs = owner ? ldcg_u32(&m.heap_size[myh]) : 0;  // this owner's heap size (private)
-    const uint32_t owner_warps = (H + 31u) / 32u;
 
     for (uint64_t it = 0;; ++it) {
         const uint32_t par = (uint32_t)(round & 1);
 
         // ------------------------------------------------ phase 1: pop ---
-        if (tid < owner_warps * 32u) {  // warps holding heap owners
+        // The owner takes the root now and refills the hole later in the
+        // round (pending_sift), off the path to the successors.
+        bool pending_sift = false;
+        E last;
+        if (tid < owner_warps * 32u) {
             E e;
             uint32_t mv = 0;
-            const bool have = owner && heap_pop<P>(myheap, hs, e);
+            const bool have = owner && hs > 0;
+            if (have) {
+                e = myheap.s[1];
+                last = myheap.ld(hs);
+                hs -= 1;
+                pending_sift = hs > 0;
+            }
             const uint64_t ecost = have ? P::entry_cost(e) : kInfCost;
             const uint64_t wmin = warp_min_cost<P>(ecost);
             if (lane == 0 && wmin != kInfCost) atomic_min_cost<P>(&st->round_min[par], wmin);
@@ -363,59 +531,64 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         const uint32_t total = scratch[0];
         __syncthreads();
 
-        // ----------------------------------- phase 1: relax successors ---
-        for (uint32_t b0 = 0; b0 < total; b0 += T) {
-            const uint32_t j = b0 + tid;
-            bool improved = false, inserted = false;
-            uint32_t nslot = 0, naux = 0, oslot = 0;
-            uint64_t ng = 0, nf = 0;
-            if (j < total) {
-                // source pop = largest h with excl[h] <= j (it has a successor)
-                uint32_t lo = 0, hi = H - 1;
-                while (lo < hi) {
-                    const uint32_t mid = (lo + hi + 1) >> 1;
-                    if (pop[mid].excl <= j)
-                        lo = mid;
-                    else
-                        hi = mid - 1;
+        // ------------------ phase 1: relax successors / refill heap roots ---
+        if (rfirst > 0 && pending_sift) heap_sift_down<P>(myheap, hs, last);
+        if (relaxer) {
+            const uint32_t rt = tid - rfirst;
+            for (uint32_t b0 = 0; b0 < total; b0 += rthreads) {
+                const uint32_t j = b0 + rt;
+                bool improved = false, inserted = false;
+                uint32_t nslot = 0, naux = 0, oslot = 0;
+                uint64_t ng = 0, nf = 0;
+                if (j < total) {
+                    // source pop = largest h with excl[h] <= j (it has a successor)
+                    uint32_t lo = 0, hi = H - 1;
+                    while (lo < hi) {
+                        const uint32_t mid = (lo + hi + 1) >> 1;
+                        if (pop[mid].excl <= j)
+                            lo = mid;
+                        else
+                            hi = mid - 1;
+                    }
+                    const PopInfo &pi = pop[lo];
+                    const int move = (int)__fns(pi.mask, 0, (int)(j - pi.excl) + 1);
+                    oslot = pi.slot;
+                    uint64_t nkey;
+                    prob.apply(pi.key, pi.g, pi.aux, move, nkey, ng, naux, nf);
+                    ++nS;
+                    const int r = relax<P>(m.tab, m.mask, m.max_probe, nkey, ng, &nslot);
+                    if (r == RELAX_FULL) {
+                        set_error(&st->error, ST_HASH_FULL);
+                    } else {
+                        inserted = (r == RELAX_INSERTED);
+                        improved = (r & RELAX_IMPROVED) != 0;
+                    }
                 }
-                const PopInfo &pi = pop[lo];
-                const int move = (int)__fns(pi.mask, 0, (int)(j - pi.excl) + 1);
-                oslot = pi.slot;
-                uint64_t nkey;
-                prob.apply(pi.key, pi.g, pi.aux, move, nkey, ng, naux, nf);
-                ++nS;
-                const int r = relax<P>(m.tab, m.mask, m.max_probe, nkey, ng, &nslot);
-                if (r == RELAX_FULL) {
-                    set_error(&st->error, ST_HASH_FULL);
-                } else {
-                    inserted = (r == RELAX_INSERTED);
-                    improved = (r & RELAX_IMPROVED) != 0;
+                const uint32_t ib = __ballot_sync(kFull, inserted);
+                if (ib && lane == (uint32_t)(__ffs(ib) - 1)) {
+                    const unsigned long long before = atomicAdd(&st->inserted, (unsigned long long)__popc(ib));
+                    if (before + __popc(ib) > m.max_inserted) set_error(&st->error, ST_HASH_FULL);
                 }
-            }
-            const uint32_t ib = __ballot_sync(kFull, inserted);
-            if (ib && lane == (uint32_t)(__ffs(ib) - 1)) {
-                const unsigned long long before = atomicAdd(&st->inserted, (unsigned long long)__popc(ib));
-                if (before + __popc(ib) > m.max_inserted) set_error(&st->error, ST_HASH_FULL);
-            }
-            const uint32_t bal = __ballot_sync(kFull, improved);
-            if (bal) {
-                const uint32_t leader = (uint32_t)(__ffs(bal) - 1);
-                uint32_t cbase = 0;
-                if (lane == leader) cbase = atomicAdd(&st->cand_count[par], (uint32_t)__popc(bal));
-                cbase = __shfl_sync(kFull, cbase, leader);
-                if (improved) {
-                    Cand c;
-                    c.slot = nslot;
-                    c.parent = oslot;
-                    c.g = ng;
-                    c.f = nf;
-                    c.aux = naux;
-                    c.pad = 0;
-                    m.cand[cbase + __popc(bal & lanemask_lt())] = c;
+                const uint32_t bal = __ballot_sync(kFull, improved);
+                if (bal) {
+                    const uint32_t leader = (uint32_t)(__ffs(bal) - 1);
+                    uint32_t cbase = 0;
+                    if (lane == leader) cbase = atomicAdd(&st->cand_count[par], (uint32_t)__popc(bal));
+                    cbase = __shfl_sync(kFull, cbase, leader);
+                    if (improved) {
+                        Cand c;
+                        c.slot = nslot;
+                        c.parent = oslot;
+                        c.g = ng;
+                        c.f = nf;
+                        c.aux = naux;
+                        c.pad = 0;
+                        m.cand[cbase + __popc(bal & lanemask_lt())] = c;
+                    }
                 }
             }
         }
+        if (rfirst == 0 && pending_sift) heap_sift_down<P>(myheap, hs, last);
 
         team.sync();
 
@@ -462,7 +635,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                 if (ldcg_u64(&m.tab[c.slot].g) != c.g) continue;  // lost to a better writer
                 m.tab[c.slot].prev = c.parent;
                 m.tab[c.slot].aux = c.aux;
-                if (hs + 1 >= m.stride) {
+                if (hs + 1 > m.hcap) {
                     set_error(&st->error2[par], ST_HEAP_OVERFLOW);
                     break;
                 }
@@ -475,10 +648,10 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         if (it + 1 >= budget) break;
     }
 
-    // Persist the resumable state.
+    // Persist the resumable state: sizes and the shared tops.
     if (owner) {
         m.heap_size[myh] = hs;
-        for (uint32_t i = 1; i <= topn && i <= hs; ++i) P::store(myheap.g + i, myheap.s[i]);
+        for (uint32_t i = 1; i <= topn && i <= hs; ++i) P::store(gblock + i, myheap.s[i]);
     }
     if (cta == 0 && tid == 0) {
         st->round = round;

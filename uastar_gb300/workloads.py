@@ -119,7 +119,8 @@ def mixed_1024(n_puzzles: int = 768, n_grids: int = 256, seed: int = MIX_SEED, m
     return specs
 
 
-def serve_stream(count: int, rate_per_s: float, seed: int = 0x5E57E, max_side: int = 8192):
+def serve_stream(count: int, rate_per_s: float, seed: int = 0x5E57E, max_side: int = 8192,
+                 walks: tuple = (60, 300), min_side: int = 256):
     """(arrival offset in seconds, spec) pairs: Poisson arrivals at `rate_per_s`."""
     t = 0.0
     out = []
@@ -127,9 +128,9 @@ def serve_stream(count: int, rate_per_s: float, seed: int = 0x5E57E, max_side: i
         u = uniform(seed, 4 * i)
         t += -math.log(1.0 - u) / rate_per_s
         if uniform(seed, 4 * i + 1) < 0.5:
-            spec = PuzzleSpec(4, randint(seed, 4 * i + 2, 60, 300), splitmix64(seed ^ 0x77, i))
+            spec = PuzzleSpec(4, randint(seed, 4 * i + 2, walks[0], walks[1]), splitmix64(seed ^ 0x77, i))
         else:
-            side = randint(seed, 4 * i + 2, 256, max_side)
+            side = randint(seed, 4 * i + 2, min_side, max_side)
             r = round(0.10 + 0.30 * uniform(seed, 4 * i + 3), 4)
             spec = screened_grid(side, side, r, splitmix64(seed ^ 0x99, i) & 0xFFFFFFFF)
         out.append((t, spec))
