@@ -268,6 +268,38 @@ int32_t uastar_serve_stop(uastar_engine *eng, double timeout_s, uastar_serve_sta
 /* CLOCK_MONOTONIC now, seconds (the clock serve_submit's arrival_s uses). */
 double uastar_now_s(void);
 
+/* ---- allocation-free grid solve ---------------------------------------- */
+/* No counterpart in the reference.  For callers that may not allocate device
+ * memory while they run (a plugin inside another framework's memory pool, a
+ * real-time or graph-replayed loop, an allocator-free service): the same GA*
+ * search as uastar_grid_solve, run out of one fixed device array the library
+ * reserves at load time (about 53 MB on every GPU that loads it, held until
+ * the process exits), so the call allocates nothing.  The caller passes device
+ * buffers: the bitmap (layout as above), a path buffer of path_cap cell ids
+ * and a result record; the call is asynchronous on `stream` (a cudaStream_t
+ * as void*, NULL = the default stream) and the result is valid once the
+ * stream has finished.  The first call on a device looks up the array's
+ * device address: make it outside any stream capture.  Grids above 2^22
+ * cells are rejected with UASTAR_BAD_INPUT; a search that outgrows the array
+ * (2^20 dedup slots at 80 % load, 256 heaps of 4095 entries) reports
+ * UASTAR_HASH_FULL or UASTAR_HEAP_OVERFLOW in the result, a path longer than
+ * path_cap UASTAR_ARENA_FULL.  All calls share the array: calls that overlap
+ * on the GPU race, so serialize them. */
+typedef struct {
+    int32_t status;
+    int32_t reserved;
+    int64_t straight;
+    int64_t diagonal;
+    int64_t expanded;
+    int64_t generated;
+    int64_t rounds;
+    int64_t path_len;         /* cells written to the path buffer, start -> goal */
+} uastar_noalloc_grid_result;
+
+int32_t uastar_grid_solve_noalloc(const uint64_t *d_words, int32_t H, int32_t W, int32_t sx, int32_t sy,
+                                  int32_t ex, int32_t ey, int32_t *d_path, int64_t path_cap,
+                                  uastar_noalloc_grid_result *d_result, void *stream);
+
 /* ---- host utilities: instance generators and path validation ---------- */
 /* Seeded Bernoulli grid: cell id is blocked iff the top 32 bits of output #id
  * of the splitmix64 stream seeded with `seed` fall below

@@ -87,6 +87,12 @@ class ServeStats(C.Structure):
                 ("peak_budget_gb", C.c_double), ("peak_resident", C.c_int32), ("reserved", C.c_int32)]
 
 
+class NoallocGridResult(C.Structure):
+    _fields_ = [("status", C.c_int32), ("reserved", C.c_int32), ("straight", C.c_int64),
+                ("diagonal", C.c_int64), ("expanded", C.c_int64), ("generated", C.c_int64),
+                ("rounds", C.c_int64), ("path_len", C.c_int64)]
+
+
 # (name, restype, argtypes) for every entry point of uastar_gpu.h
 _P = C.c_void_p
 _U64P = C.POINTER(C.c_uint64)
@@ -122,6 +128,8 @@ SIGNATURES = [
     ("uastar_serve_cancel", C.c_int32, [_P, C.c_int64]),
     ("uastar_serve_stop", C.c_int32, [_P, C.c_double, C.POINTER(ServeStats)]),
     ("uastar_now_s", C.c_double, []),
+    ("uastar_grid_solve_noalloc", C.c_int32, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                              C.c_int32, _P, C.c_int64, _P, _P]),
     ("uastar_gen_grid", C.c_int32, [C.c_uint64, C.c_int32, C.c_int32, C.c_double, C.c_int32, C.c_int32,
                                     C.c_int32, C.c_int32, _U64P]),
     ("uastar_gen_puzzle", C.c_int32, [C.c_uint64, C.c_int32, C.c_int32, _U8P]),

@@ -19,7 +19,7 @@ OUT_DIR = PKG / "_build"
 LIB = PKG / "libuastar_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["engine.cu", "pdb.cu", "batch.cu"]
+CUDA_SOURCES = ["engine.cu", "pdb.cu", "batch.cu", "noalloc.cu"]
 HOST_SOURCES = ["host_utils.cpp"]
 
 
