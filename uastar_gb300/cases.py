@@ -1,0 +1,56 @@
+"""Run one named workload case on the engine (for profiling and quick checks).
+
+    python -m uastar_gb300.cases grid_1000 [--repeat 2]
+    python -m uastar_gb300.cases grid_20000 [--repeat 2]
+    python -m uastar_gb300.cases puzzle15 [--count 10]
+    python -m uastar_gb300.cases mixed_small [--repeat 1]
+
+Each repeat solves the case once and prints one line of results; profilers
+capture the second launch of the search kernel (`-s 1 -c 1`).
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+from . import Engine
+from . import workloads as WL
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case", choices=["grid_1000", "grid_20000", "puzzle15", "mixed_small"])
+    ap.add_argument("--repeat", type=int, default=2)
+    ap.add_argument("--count", type=int, default=10)
+    args = ap.parse_args()
+
+    if args.case in ("grid_1000", "grid_20000"):
+        sp = WL.GRID_1000 if args.case == "grid_1000" else WL.GRID_20000
+        kw = {"hash_log2_slots": 28} if args.case == "grid_20000" else {}
+        words = sp.words()
+        with Engine(0, heaps=8192, block_threads=256, threads_per_heap=4, **kw) as eng:
+            for _ in range(args.repeat):
+                r = eng.grid_solve(words, sp.H, sp.W, sp.start, sp.goal)
+                print(f"{args.case}: {r.straight}+{r.diagonal}*sqrt2 cost {r.cost:.4f} expanded {r.expanded} "
+                      f"rounds {r.rounds} kernel {r.kernel_ms:.1f} ms", flush=True)
+    elif args.case == "puzzle15":
+        with Engine(0) as eng:
+            eng.pdb_build(4)
+            for _ in range(args.repeat):
+                t0 = time.perf_counter()
+                steps = [eng.puzzle_solve(4, s.tiles()).steps for s in WL.puzzle15_x100(count=args.count)]
+                print(f"puzzle15: {len(steps)} solves in {time.perf_counter() - t0:.3f} s, steps {steps}", flush=True)
+    else:
+        specs = [WL.PuzzleSpec(4, 60 + i, 7000 + i) for i in range(48)]
+        specs += [WL.screened_grid(256 + 32 * i, 256 + 32 * i, 0.25, 11 + i, exact=True) for i in range(8)]
+        insts = [s.instance() for s in specs]
+        with Engine(0) as eng:
+            eng.pdb_build(4)
+            for _ in range(args.repeat):
+                res, st = eng.batch_solve(insts)
+                print(f"mixed_small: {sum(r['status'] == 0 for r in res)}/{len(res)} ok, "
+                      f"{st['wall_ms']:.1f} ms, waves {st['waves']}", flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -328,6 +328,18 @@ int32_t grid_solve_impl(uastar_engine *eng, const uint64_t *host_words, int32_t 
         for (size_t i = 0; i < keys.size(); ++i) eng->path[i] = (int32_t)keys[i];
         eng->path_cached = true;
         out->path_len = (int64_t)keys.size();
+        // float32 g accumulated along the path in order, as the reference's
+        // CPU solver computes it (CPU-solver.cpp:105)
+        {
+            const float sqrt2f = 1.4142135623731f;
+            float fc = 0.0f;
+            for (size_t i = 1; i < eng->path.size(); ++i) {
+                const int64_t u = eng->path[i - 1], v = eng->path[i];
+                const bool diag = (u / W != v / W) && (u % W != v % W);
+                fc = fc + (diag ? sqrt2f : 1.0f);
+            }
+            out->cost = fc;
+        }
         if (host_words) {
             int64_t a = 0, b = 0;
             float fc = 0;
