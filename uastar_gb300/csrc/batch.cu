@@ -212,16 +212,28 @@ __global__ void __launch_bounds__(512, 1) k_batch_cluster(BatchArgs a) {
     uint8_t *heaps = a.heaps + (size_t)cid * csize * H * a.slice;
     uint32_t *hs = a.hsize + (size_t)cid * csize * H;
     Cand *cand = a.cand + (size_t)cid * csize * H * 8;
-    for (;;) {
-        if (crank == 0 && threadIdx.x == 0) a.cnext[cid] = atomicAdd(a.queue, 1u);
-        team.sync();
-        const uint32_t i = ldcg_u32(&a.cnext[cid]);
+    for (uint32_t iter = 0;; ++iter) {
+        uint32_t i;
+        if (a.serving) {
+            // serving: cluster c advances large-request slot c by one quantum
+            if (iter > 0) break;
+            i = cid;
+        } else {
+            if (crank == 0 && threadIdx.x == 0) a.cnext[cid] = atomicAdd(a.queue, 1u);
+            team.sync();
+            i = ldcg_u32(&a.cnext[cid]);
+        }
         if (i >= a.count) break;
         const InstDesc d = a.descs[i];
+        if (a.serving && d.kind == 0) break;  // empty slot
+        if (a.serving) heaps = a.heaps + d.heap_off;
         const unsigned long long t_start = globaltimer_ns();
-        clear_partition_team(a.tab + d.tab_off, 1ull << d.log2_slots, crank, csize);
-        for (uint32_t j = threadIdx.x; j < H; j += blockDim.x) hs[crank * H + j] = 0;
-        if (crank == 0 && threadIdx.x == 0) init_state(st);
+        if (!a.serving || d.fresh) {
+            // serving partitions are cleared by the host at admission (fresh == 2)
+            if (d.fresh != 2) clear_partition_team(a.tab + d.tab_off, 1ull << d.log2_slots, crank, csize);
+            for (uint32_t j = threadIdx.x; j < H; j += blockDim.x) hs[crank * H + j] = 0;
+            if (crank == 0 && threadIdx.x == 0) init_state(st);
+        }
         team.sync();
         run_instance(a, d, team, heaps, hs, cand, smem, a.budget);
         team.sync();
@@ -952,23 +964,44 @@ struct ServeReq {
     uastar_instance inst{};
     std::vector<uint64_t> words;  // owned copy of the grid bitmap
     double arrival_s = 0;
-    uint64_t mult = 1;            // dedup partition growth after HASH_FULL
+    uint64_t mult = 1;            // dedup partition growth (overflow, promotion)
     uint32_t heap_mult = 1;       // heap slice growth after HEAP_OVERFLOW
     int attempts = 0;
+    bool large = false;           // runs on a cluster slot
     uastar_instance_result acc{};
 };
 
-struct ServeSlotState {
+struct ServeSlot {
     bool busy = false;
     ServeReq req;
     uint64_t tab_off = 0, tab_n = 0, bm_off = 0, bm_n = 0, heap_off = 0, heap_n = 0;
 };
 
+// One kind of resident slot: single CTAs (small requests) or 8-CTA clusters
+// (large requests).  Each tier has its own quantum kernel and stream; the two
+// kernels run side by side.
+struct ServeTier {
+    bool large = false;
+    int nslots = 0;
+    BatchGeometry geo{};
+    std::vector<ServeSlot> slots;
+    std::vector<InstDesc> descs;
+    std::vector<InstOut> outs;
+    DevBuf d_descs, d_outs, d_states, d_hsize, d_cand, d_walk;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int resident() const {
+        int n = 0;
+        for (auto &sl : slots) n += sl.busy;
+        return n;
+    }
+};
+
 struct ServeState {
     uastar_engine *eng = nullptr;
     uastar_serve_config cfg{};
-    int T = 256, S = 0;
-    BatchGeometry geo{};
+    ServeTier tier[2];  // 0 = CTA slots, 1 = cluster slots
+    uint64_t promote_rounds = 4096;
     uint64_t heap_bytes = 0;
     std::thread th;
     std::mutex mu;
@@ -981,11 +1014,9 @@ struct ServeState {
     int64_t outstanding = 0;  // submitted and not yet completed
     uastar_serve_stats stats{};
     int32_t loop_error = UASTAR_OK;
-    // device state
-    DevBuf tab, bitmaps, heaps, hsize, cand, descs, outs, states, walk;
-    RangeAlloc tab_alloc, bm_alloc, heap_alloc;  // units: slots, 8-byte words, 16-byte heap entries
-    cudaStream_t stream = nullptr;
-    cudaEvent_t q0 = nullptr, q1 = nullptr;
+    // device arenas shared by both tiers
+    DevBuf tab, bitmaps, heaps;
+    RangeAlloc tab_alloc, bm_alloc, heap_alloc;  // units: slots, 8-byte words, 16-byte heap units
 };
 
 static void serve_complete(ServeState *S, ServeReq &r, int32_t status) {
@@ -1009,21 +1040,126 @@ static uint64_t serve_partition_slots(const ServeState *S, const ServeReq &r) {
     return std::max<uint64_t>(slots, 1u << 12);
 }
 
+static void serve_release(ServeState *S, ServeSlot &sl) {
+    S->tab_alloc.release(sl.tab_off, sl.tab_n);
+    if (sl.bm_n) S->bm_alloc.release(sl.bm_off, sl.bm_n);
+    S->heap_alloc.release(sl.heap_off, sl.heap_n);
+}
+
+// Try to place `r` in a free slot of tier `t`.  Returns 1 placed, 0 no room
+// now, -1 can never fit (completed as REJECTED by the caller).
+static int serve_admit(ServeState *S, ServeTier &t, ServeReq &r) {
+    uastar_engine *eng = S->eng;
+    int free_slot = -1;
+    for (int q = 0; q < t.nslots; ++q)
+        if (!t.slots[q].busy) {
+            free_slot = q;
+            break;
+        }
+    if (free_slot < 0) return 0;
+    const uint64_t tn = serve_partition_slots(S, r);
+    const uint64_t bn = r.inst.kind == UASTAR_KIND_GRID ? r.words.size() + 2 : 0;
+    BatchGeometry hgeo = t.geo;
+    hgeo.set_capacity((t.geo.want + 1) * r.heap_mult - 1);
+    const bool grid = r.inst.kind == UASTAR_KIND_GRID;
+    const uint32_t hstride = grid ? hgeo.hg_grid.stride : hgeo.hg_puzzle.stride;
+    const uint32_t hhcap = grid ? hgeo.hg_grid.hcap : hgeo.hg_puzzle.hcap;
+    const uint64_t heaps_per_req = (uint64_t)t.geo.H * (t.large ? 8 : 1);
+    const uint64_t hn = (heaps_per_req * hstride * (grid ? 16 : 8) + 127) / 128 * 8;  // 16-byte units
+    if (tn > S->tab_alloc.capacity() || bn > S->bm_alloc.capacity() || hn > S->heap_alloc.capacity()) return -1;
+    uint64_t toff = 0, boff = 0, hoff = 0;
+    if (!S->tab_alloc.alloc(tn, 4, &toff)) return 0;
+    if (bn && !S->bm_alloc.alloc(bn, 2, &boff)) {
+        S->tab_alloc.release(toff, tn);
+        return 0;
+    }
+    if (!S->heap_alloc.alloc(hn, 8, &hoff)) {
+        S->tab_alloc.release(toff, tn);
+        if (bn) S->bm_alloc.release(boff, bn);
+        return 0;
+    }
+    ServeSlot &sl = t.slots[free_slot];
+    sl.busy = true;
+    sl.tab_off = toff;
+    sl.tab_n = tn;
+    sl.bm_off = boff;
+    sl.bm_n = bn;
+    sl.heap_off = hoff;
+    sl.heap_n = hn;
+    sl.req = std::move(r);
+    sl.req.attempts += 1;
+    InstDesc d;
+    std::memset(&d, 0, sizeof d);
+    d.kind = sl.req.inst.kind;
+    d.n = sl.req.inst.n;
+    d.max_rounds = eng->cfg.max_rounds;
+    d.tab_off = toff;
+    d.log2_slots = (uint32_t)log2_u64(tn);
+    d.fresh = 2;  // cleared here, at admission, by a full-GPU fill
+    d.heap_off = hoff * 16;
+    d.heap_stride = hstride;
+    d.heap_hcap = hhcap;
+    if (fill_ff_async(eng, S->tab.as<Slot>() + toff, tn * sizeof(Slot), t.stream) != UASTAR_OK) {
+        S->loop_error = UASTAR_CUDA_ERROR;
+        return 0;
+    }
+    if (d.kind == UASTAR_KIND_GRID) {
+        d.H = sl.req.inst.H;
+        d.W = sl.req.inst.W;
+        d.sx = sl.req.inst.sx;
+        d.sy = sl.req.inst.sy;
+        d.ex = sl.req.inst.ex;
+        d.ey = sl.req.inst.ey;
+        d.bm_word = boff * 2;
+        if (cudaMemcpyAsync(S->bitmaps.as<uint64_t>() + boff, sl.req.words.data(), sl.req.words.size() * 8,
+                            cudaMemcpyHostToDevice, t.stream) != cudaSuccess)
+            S->loop_error = UASTAR_CUDA_ERROR;
+    } else {
+        d.start_key = pack_board(d.n, sl.req.inst.tiles);
+    }
+    t.descs[free_slot] = d;
+    return 1;
+}
+
+static BatchArgs serve_args(ServeState *S, ServeTier &t) {
+    BatchArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.descs = t.d_descs.as<InstDesc>();
+    a.count = (uint32_t)t.nslots;
+    a.bitmaps = S->bitmaps.as<uint32_t>();
+    a.pdb3 = S->eng->pdb[3].as<uint8_t>();
+    a.pdb4 = S->eng->pdb[4].as<uint8_t>();
+    a.tab = S->tab.as<Slot>();
+    a.heaps = S->heaps.as<uint8_t>();
+    a.slice = t.geo.slice;
+    a.hsize = t.d_hsize.as<uint32_t>();
+    a.cand = t.d_cand.as<Cand>();
+    a.outs = t.d_outs.as<InstOut>();
+    if (t.large)
+        a.cstates = t.d_states.as<TeamState>();
+    else
+        a.states = t.d_states.as<TeamState>();
+    a.max_load = 0.75;
+    a.H = t.geo.H;
+    a.L_grid = t.geo.L_grid;
+    a.L_puzzle = t.geo.L_puzzle;
+    a.budget = (uint64_t)(S->cfg.rounds_per_quantum > 0 ? S->cfg.rounds_per_quantum : 256);
+    a.serving = 1;
+    return a;
+}
+
 static void serve_loop(ServeState *S) {
     uastar_engine *eng = S->eng;
     cudaSetDevice(eng->device);
-    std::vector<ServeSlotState> slots(S->S);
-    std::vector<ServeReq> pending;  // kept sorted by arrival
-    std::vector<InstDesc> descs(S->S);
-    std::vector<InstOut> outs(S->S);
-    std::memset(descs.data(), 0, descs.size() * sizeof(InstDesc));
+    std::vector<ServeReq> pending;   // arrived or future requests, sorted by arrival
+    std::deque<ServeReq> promoted;   // requests waiting for a cluster slot
     cudaError_t e;
     auto fail = [&](cudaError_t err, const char *what) {
         fail_cuda(eng, err, what);
         S->loop_error = UASTAR_CUDA_ERROR;
     };
     for (;;) {
-        // 1. intake
+        // 1. intake and cancellation
         {
             std::unique_lock<std::mutex> lk(S->mu);
             while (!S->incoming.empty()) {
@@ -1042,102 +1178,49 @@ static void serve_loop(ServeState *S) {
                         pending.erase(pending.begin() + i);
                         break;
                     }
-                for (int s = 0; s < S->S; ++s)
-                    if (slots[s].busy && slots[s].req.id == cid) {
-                        serve_complete(S, slots[s].req, UASTAR_CANCELLED);
-                        S->tab_alloc.release(slots[s].tab_off, slots[s].tab_n);
-                        if (slots[s].bm_n) S->bm_alloc.release(slots[s].bm_off, slots[s].bm_n);
-                        S->heap_alloc.release(slots[s].heap_off, slots[s].heap_n);
-                        slots[s] = ServeSlotState();
-                        descs[s].kind = 0;
+                for (size_t i = 0; i < promoted.size(); ++i)
+                    if (promoted[i].id == cid) {
+                        serve_complete(S, promoted[i], UASTAR_CANCELLED);
+                        promoted.erase(promoted.begin() + i);
+                        break;
                     }
+                for (auto &t : S->tier)
+                    for (int q = 0; q < t.nslots; ++q)
+                        if (t.slots[q].busy && t.slots[q].req.id == cid) {
+                            serve_complete(S, t.slots[q].req, UASTAR_CANCELLED);
+                            serve_release(S, t.slots[q]);
+                            t.slots[q] = ServeSlot();
+                            t.descs[q].kind = 0;
+                        }
             }
         }
         if (S->loop_error) break;
-        // 2. admission: arrived requests, in arrival order, while a slot and budget are free
+        // 2. admission: promoted requests into cluster slots, arrived ones into CTA slots
+        ServeTier &small = S->tier[0], &large = S->tier[1];
+        while (!promoted.empty() && large.nslots > 0) {
+            const int r = serve_admit(S, large, promoted.front());
+            if (r == 0) break;
+            if (r < 0) serve_complete(S, promoted.front(), UASTAR_REJECTED);
+            promoted.pop_front();
+        }
         const double now = uastar_now_s();
         size_t taken = 0;
-        int free_slot = 0;
         for (; taken < pending.size(); ++taken) {
             ServeReq &r = pending[taken];
             if (r.arrival_s > now) break;
-            while (free_slot < S->S && slots[free_slot].busy) ++free_slot;
-            if (free_slot >= S->S) break;
-            const uint64_t tn = serve_partition_slots(S, r);
-            const uint64_t bn = r.inst.kind == UASTAR_KIND_GRID ? r.words.size() + 2 : 0;
-            // heap slice: H heaps of the request's entry type, grown 8x per overflow
-            BatchGeometry hgeo = S->geo;
-            hgeo.set_capacity((S->geo.want + 1) * r.heap_mult - 1);
-            const bool grid = r.inst.kind == UASTAR_KIND_GRID;
-            const uint32_t hstride = grid ? hgeo.hg_grid.stride : hgeo.hg_puzzle.stride;
-            const uint32_t hhcap = grid ? hgeo.hg_grid.hcap : hgeo.hg_puzzle.hcap;
-            const uint64_t hn = ((uint64_t)S->geo.H * hstride * (grid ? 16 : 8) + 127) / 128 * 8;  // 16-byte units
-            if (tn > S->tab_alloc.capacity() || bn > S->bm_alloc.capacity() || hn > S->heap_alloc.capacity()) {
-                serve_complete(S, r, UASTAR_REJECTED);  // can never fit the budget
-                continue;
-            }
-            uint64_t toff = 0, boff = 0, hoff = 0;
-            if (!S->tab_alloc.alloc(tn, 4, &toff)) break;  // wait for memory to free up
-            if (bn && !S->bm_alloc.alloc(bn, 2, &boff)) {
-                S->tab_alloc.release(toff, tn);
-                break;
-            }
-            if (!S->heap_alloc.alloc(hn, 8, &hoff)) {
-                S->tab_alloc.release(toff, tn);
-                if (bn) S->bm_alloc.release(boff, bn);
-                break;
-            }
-            ServeSlotState &sl = slots[free_slot];
-            sl.busy = true;
-            sl.tab_off = toff;
-            sl.tab_n = tn;
-            sl.bm_off = boff;
-            sl.bm_n = bn;
-            sl.heap_off = hoff;
-            sl.heap_n = hn;
-            sl.req = std::move(r);
-            sl.req.attempts += 1;
-            InstDesc d;
-            std::memset(&d, 0, sizeof d);
-            d.kind = sl.req.inst.kind;
-            d.n = sl.req.inst.n;
-            d.max_rounds = eng->cfg.max_rounds;
-            d.tab_off = toff;
-            d.log2_slots = (uint32_t)log2_u64(tn);
-            d.fresh = 2;
-            if (fill_ff_async(eng, S->tab.as<Slot>() + toff, tn * sizeof(Slot), S->stream) != UASTAR_OK) {
-                S->loop_error = UASTAR_CUDA_ERROR;
-                break;
-            }
-            d.heap_off = hoff * 16;
-            d.heap_stride = hstride;
-            d.heap_hcap = hhcap;
-            if (d.kind == UASTAR_KIND_GRID) {
-                d.H = sl.req.inst.H;
-                d.W = sl.req.inst.W;
-                d.sx = sl.req.inst.sx;
-                d.sy = sl.req.inst.sy;
-                d.ex = sl.req.inst.ex;
-                d.ey = sl.req.inst.ey;
-                d.bm_word = boff * 2;
-                e = cudaMemcpyAsync(S->bitmaps.as<uint64_t>() + boff, sl.req.words.data(),
-                                    sl.req.words.size() * 8, cudaMemcpyHostToDevice, S->stream);
-                if (e != cudaSuccess) fail(e, "serve bitmap upload");
-            } else {
-                d.start_key = pack_board(d.n, sl.req.inst.tiles);
-            }
-            descs[free_slot] = d;
+            const int a = serve_admit(S, small, r);
+            if (a == 0) break;
+            if (a < 0) serve_complete(S, r, UASTAR_REJECTED);
         }
         pending.erase(pending.begin(), pending.begin() + taken);
-        int resident = 0;
-        for (auto &sl : slots) resident += sl.busy;
-        S->stats.peak_resident = std::max(S->stats.peak_resident, resident);
+        const int rs = small.resident(), rl = large.resident();
+        S->stats.peak_resident = std::max(S->stats.peak_resident, rs + rl);
         S->stats.peak_budget_gb =
             std::max(S->stats.peak_budget_gb, ((double)S->tab_alloc.used() * sizeof(Slot) +
-                                               (double)S->bm_alloc.used() * 8 +
-                                               (double)S->heap_alloc.used() * 16) /
+                                               (double)S->bm_alloc.used() * 8 + (double)S->heap_alloc.used() * 16) /
                                                   1e9);
-        if (resident == 0) {
+        if (S->loop_error) break;
+        if (rs + rl == 0) {
             std::unique_lock<std::mutex> lk(S->mu);
             if (S->abort_now || (S->draining && S->outstanding == 0)) break;
             double wait_s = 0.002;
@@ -1146,166 +1229,222 @@ static void serve_loop(ServeState *S) {
                 S->cv.wait_for(lk, std::chrono::duration<double>(wait_s));
             continue;
         }
-        // 3. one quantum over all resident requests
-        if ((e = cudaMemcpyAsync(S->descs.p, descs.data(), S->S * sizeof(InstDesc), cudaMemcpyHostToDevice,
-                                 S->stream)) != cudaSuccess) {
-            fail(e, "serve desc upload");
-            break;
+        // 3. one quantum: the cluster tier first (it needs whole GPCs), then the CTA tier
+        for (int ti = 1; ti >= 0; --ti) {
+            ServeTier &t = S->tier[ti];
+            if (!t.resident()) continue;
+            if ((e = cudaMemcpyAsync(t.d_descs.p, t.descs.data(), t.nslots * sizeof(InstDesc),
+                                     cudaMemcpyHostToDevice, t.stream)) != cudaSuccess) {
+                fail(e, "serve desc upload");
+                break;
+            }
+            BatchArgs a = serve_args(S, t);
+            cudaEventRecord(t.e0, t.stream);
+            if (t.large) {
+                cudaLaunchConfig_t lc = {};
+                cudaLaunchAttribute lat[1];
+                lat[0].id = cudaLaunchAttributeClusterDimension;
+                lat[0].val.clusterDim.x = 8;
+                lat[0].val.clusterDim.y = 1;
+                lat[0].val.clusterDim.z = 1;
+                lc.gridDim = dim3((unsigned)(t.nslots * 8));
+                lc.blockDim = dim3((unsigned)t.geo.T);
+                lc.dynamicSmemBytes = t.geo.smem;
+                lc.stream = t.stream;
+                lc.attrs = lat;
+                lc.numAttrs = 1;
+                e = cudaLaunchKernelEx(&lc, k_batch_cluster, a);
+            } else {
+                k_batch<<<t.nslots, t.geo.T, t.geo.smem, t.stream>>>(a);
+                e = cudaGetLastError();
+            }
+            eng->launches++;
+            cudaEventRecord(t.e1, t.stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(t.outs.data(), t.d_outs.p, t.nslots * sizeof(InstOut), cudaMemcpyDeviceToHost,
+                                    t.stream);
+            if (e != cudaSuccess) {
+                fail(e, "serve quantum");
+                break;
+            }
         }
-        BatchArgs a;
-        std::memset(&a, 0, sizeof a);
-        a.descs = S->descs.as<InstDesc>();
-        a.count = (uint32_t)S->S;
-        a.bitmaps = S->bitmaps.as<uint32_t>();
-        a.pdb3 = eng->pdb[3].as<uint8_t>();
-        a.pdb4 = eng->pdb[4].as<uint8_t>();
-        a.tab = S->tab.as<Slot>();
-        a.heaps = S->heaps.as<uint8_t>();
-        a.hsize = S->hsize.as<uint32_t>();
-        a.cand = S->cand.as<Cand>();
-        a.outs = S->outs.as<InstOut>();
-        a.states = S->states.as<TeamState>();
-        a.max_load = 0.75;
-        a.H = S->geo.H;
-        a.L_grid = S->geo.L_grid;
-        a.L_puzzle = S->geo.L_puzzle;
-        a.budget = (uint64_t)(S->cfg.rounds_per_quantum > 0 ? S->cfg.rounds_per_quantum : 256);
-        a.serving = 1;
-        cudaEventRecord(S->q0, S->stream);
-        k_batch<<<S->S, S->T, S->geo.smem, S->stream>>>(a);
-        eng->launches++;
-        cudaEventRecord(S->q1, S->stream);
-        e = cudaGetLastError();
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(outs.data(), S->outs.p, S->S * sizeof(InstOut), cudaMemcpyDeviceToHost, S->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(S->stream);
-        if (e != cudaSuccess) {
-            fail(e, "serve quantum");
-            break;
-        }
+        if (S->loop_error) break;
         float qms = 0;
-        cudaEventElapsedTime(&qms, S->q0, S->q1);
+        for (auto &t : S->tier) {
+            if (!t.resident()) continue;
+            if ((e = cudaStreamSynchronize(t.stream)) != cudaSuccess) {
+                fail(e, "serve quantum");
+                break;
+            }
+            float ms = 0;
+            cudaEventElapsedTime(&ms, t.e0, t.e1);
+            qms = std::max(qms, ms);
+        }
+        if (S->loop_error) break;
         S->stats.quanta += 1;
         S->stats.busy_ms += qms;
-        // 4. retire finished requests
-        std::vector<uint32_t> which;
-        std::vector<uint64_t> koff, kcap;
-        uint64_t ktot = 0;
-        for (int s = 0; s < S->S; ++s) {
-            if (!slots[s].busy) continue;
-            descs[s].fresh = 0;
-            if (outs[s].status == ST_RUNNING) continue;
-            if (outs[s].status == ST_OK) {
-                const auto &in = slots[s].req.inst;
-                const uint64_t cap = in.kind == UASTAR_KIND_GRID ? 8ull * (in.H + in.W) + 64 : 512;
-                which.push_back((uint32_t)s);
-                koff.push_back(ktot);
-                kcap.push_back(cap);
-                ktot += cap;
-            }
-        }
-        std::vector<unsigned long long> keys(ktot), lens(which.size());
-        if (!which.empty()) {
-            const size_t nw = which.size();
-            if ((e = S->walk.ensure(ktot * 8 + nw * 32 + 256)) != cudaSuccess) {
-                fail(e, "serve walk alloc");
-                break;
-            }
-            char *base = S->walk.as<char>();
-            unsigned long long *d_keys = reinterpret_cast<unsigned long long *>(base);
-            uint64_t *d_off = reinterpret_cast<uint64_t *>(base + ktot * 8);
-            uint64_t *d_cap = d_off + nw;
-            unsigned long long *d_len = reinterpret_cast<unsigned long long *>(d_cap + nw);
-            uint32_t *d_which = reinterpret_cast<uint32_t *>(d_len + nw);
-            cudaMemcpyAsync(d_off, koff.data(), nw * 8, cudaMemcpyHostToDevice, S->stream);
-            cudaMemcpyAsync(d_cap, kcap.data(), nw * 8, cudaMemcpyHostToDevice, S->stream);
-            cudaMemcpyAsync(d_which, which.data(), nw * 4, cudaMemcpyHostToDevice, S->stream);
-            k_batch_walk<<<(unsigned)((nw + 127) / 128), 128, 0, S->stream>>>(
-                S->descs.as<InstDesc>(), S->outs.as<InstOut>(), d_which, (uint32_t)nw, S->tab.as<Slot>(), d_keys,
-                d_off, d_cap, d_len);
-            eng->launches++;
-            cudaMemcpyAsync(lens.data(), d_len, nw * 8, cudaMemcpyDeviceToHost, S->stream);
-            cudaMemcpyAsync(keys.data(), d_keys, ktot * 8, cudaMemcpyDeviceToHost, S->stream);
-            if ((e = cudaStreamSynchronize(S->stream)) != cudaSuccess) {
-                fail(e, "serve walk");
-                break;
-            }
-        }
-        std::vector<int> walk_of(S->S, -1);
-        for (size_t w = 0; w < which.size(); ++w) walk_of[which[w]] = (int)w;
-        for (int s = 0; s < S->S; ++s) {
-            ServeSlotState &sl = slots[s];
-            if (!sl.busy || outs[s].status == ST_RUNNING) continue;
-            const InstOut &o = outs[s];
-            ServeReq &r = sl.req;
-            r.acc.device_ms = (double)(o.t_end - o.t_start) * 1e-6;
-            r.acc.expanded += (int64_t)o.expanded;
-            r.acc.generated += (int64_t)o.generated;
-            r.acc.rounds += (int64_t)o.rounds;
-            int32_t status = (int32_t)o.status;
-            S->tab_alloc.release(sl.tab_off, sl.tab_n);
-            if (sl.bm_n) S->bm_alloc.release(sl.bm_off, sl.bm_n);
-            S->heap_alloc.release(sl.heap_off, sl.heap_n);
-            descs[s].kind = 0;
-            if ((status == ST_HASH_FULL || status == ST_HEAP_OVERFLOW) && r.attempts < 10) {
-                // re-queue with 4x the space, ahead of later arrivals
-                if (status == ST_HASH_FULL) r.mult *= 4;
-                else r.heap_mult *= 16;
-                pending.insert(pending.begin(), std::move(r));
-                sl = ServeSlotState();
-                continue;
-            }
-            if (status == ST_OK) {
-                const int w = walk_of[s];
-                const uint64_t len = lens[w];
-                const unsigned long long *kk = keys.data() + koff[w];
-                const auto &in = r.inst;
-                if (len > kcap[w]) {
-                    status = UASTAR_ARENA_FULL;
-                } else if (in.kind == UASTAR_KIND_GRID) {
-                    r.acc.straight = (int64_t)(o.goal_best >> 32);
-                    r.acc.diagonal = (int64_t)(o.goal_best & 0xffffffffu);
-                    std::vector<int32_t> path(len);
-                    for (uint64_t t = 0; t < len; ++t) path[t] = (int32_t)kk[len - 1 - t];
-                    int64_t a2 = 0, b2 = 0;
-                    float fc = 0;
-                    if (uastar_validate_grid_path(r.words.data(), in.H, in.W, in.sx, in.sy, in.ex, in.ey,
-                                                  path.data(), (int64_t)len, &a2, &b2, &fc) != UASTAR_OK ||
-                        a2 != r.acc.straight || b2 != r.acc.diagonal)
-                        status = UASTAR_CUDA_ERROR;
-                    r.acc.cost = fc;
-                } else {
-                    r.acc.steps = (int32_t)o.goal_best;
-                    std::vector<int32_t> moves;
-                    auto blank = [&](uint64_t k) {
-                        for (int c = 0; c < in.n * in.n; ++c)
-                            if (((k >> (4 * c)) & 15) == 0) return c;
-                        return -1;
-                    };
-                    for (uint64_t t = len - 1; t >= 1; --t) {
-                        const int pb = blank(kk[t]), cb = blank(kk[t - 1]);
-                        moves.push_back(cb - pb == in.n ? 0 : cb - pb == -in.n ? 1 : cb - pb == 1 ? 2 : 3);
+        // 4. retire, promote or re-queue
+        for (int ti = 0; ti < 2; ++ti) {
+            ServeTier &t = S->tier[ti];
+            std::vector<uint32_t> which;
+            std::vector<uint64_t> koff, kcap;
+            uint64_t ktot = 0;
+            for (int q = 0; q < t.nslots; ++q) {
+                ServeSlot &sl = t.slots[q];
+                if (!sl.busy) continue;
+                t.descs[q].fresh = 0;
+                const InstOut &o = t.outs[q];
+                if (o.status == ST_RUNNING) {
+                    if (!t.large && o.rounds >= S->promote_rounds && large.nslots > 0) {
+                        // large after all: restart it on a cluster slot with more space
+                        ServeReq r = std::move(sl.req);
+                        r.acc.expanded += (int64_t)o.expanded;
+                        r.acc.rounds += (int64_t)o.rounds;
+                        r.mult = std::max<uint64_t>(r.mult * 16, 16);
+                        r.large = true;
+                        serve_release(S, sl);
+                        sl = ServeSlot();
+                        t.descs[q].kind = 0;
+                        promoted.push_back(std::move(r));
                     }
-                    if ((int64_t)moves.size() != r.acc.steps ||
-                        uastar_validate_puzzle_moves(in.n, in.tiles, moves.data(), (int64_t)moves.size()) !=
-                            UASTAR_OK)
-                        status = UASTAR_CUDA_ERROR;
+                    continue;
+                }
+                if (o.status == ST_OK) {
+                    const auto &in = sl.req.inst;
+                    which.push_back((uint32_t)q);
+                    koff.push_back(ktot);
+                    const uint64_t cap = in.kind == UASTAR_KIND_GRID ? 8ull * (in.H + in.W) + 64 : 512;
+                    kcap.push_back(cap);
+                    ktot += cap;
                 }
             }
-            serve_complete(S, r, status);
-            sl = ServeSlotState();
+            std::vector<unsigned long long> keys(ktot), lens(which.size());
+            if (!which.empty()) {
+                const size_t nw = which.size();
+                if ((e = t.d_walk.ensure(ktot * 8 + nw * 32 + 256)) != cudaSuccess) {
+                    fail(e, "serve walk alloc");
+                    break;
+                }
+                char *base = t.d_walk.as<char>();
+                unsigned long long *d_keys = reinterpret_cast<unsigned long long *>(base);
+                uint64_t *d_off = reinterpret_cast<uint64_t *>(base + ktot * 8);
+                uint64_t *d_cap = d_off + nw;
+                unsigned long long *d_len = reinterpret_cast<unsigned long long *>(d_cap + nw);
+                uint32_t *d_which = reinterpret_cast<uint32_t *>(d_len + nw);
+                cudaMemcpyAsync(d_off, koff.data(), nw * 8, cudaMemcpyHostToDevice, t.stream);
+                cudaMemcpyAsync(d_cap, kcap.data(), nw * 8, cudaMemcpyHostToDevice, t.stream);
+                cudaMemcpyAsync(d_which, which.data(), nw * 4, cudaMemcpyHostToDevice, t.stream);
+                k_batch_walk<<<(unsigned)((nw + 127) / 128), 128, 0, t.stream>>>(
+                    t.d_descs.as<InstDesc>(), t.d_outs.as<InstOut>(), d_which, (uint32_t)nw, S->tab.as<Slot>(),
+                    d_keys, d_off, d_cap, d_len);
+                eng->launches++;
+                cudaMemcpyAsync(lens.data(), d_len, nw * 8, cudaMemcpyDeviceToHost, t.stream);
+                cudaMemcpyAsync(keys.data(), d_keys, ktot * 8, cudaMemcpyDeviceToHost, t.stream);
+                if ((e = cudaStreamSynchronize(t.stream)) != cudaSuccess) {
+                    fail(e, "serve walk");
+                    break;
+                }
+            }
+            std::vector<int> walk_of(t.nslots, -1);
+            for (size_t w = 0; w < which.size(); ++w) walk_of[which[w]] = (int)w;
+            for (int q = 0; q < t.nslots; ++q) {
+                ServeSlot &sl = t.slots[q];
+                if (!sl.busy || t.outs[q].status == ST_RUNNING) continue;
+                const InstOut &o = t.outs[q];
+                ServeReq &r = sl.req;
+                r.acc.device_ms = (double)(o.t_end - o.t_start) * 1e-6;
+                r.acc.expanded += (int64_t)o.expanded;
+                r.acc.generated += (int64_t)o.generated;
+                r.acc.rounds += (int64_t)o.rounds;
+                int32_t status = (int32_t)o.status;
+                serve_release(S, sl);
+                t.descs[q].kind = 0;
+                if (status == ST_HASH_FULL || status == ST_HEAP_OVERFLOW) {
+                    if (!t.large && large.nslots > 0) {
+                        r.mult = std::max<uint64_t>(r.mult * 16, 16);  // promote to a cluster slot
+                        if (status == ST_HEAP_OVERFLOW) r.heap_mult *= 2;
+                        r.large = true;
+                        promoted.push_back(std::move(r));
+                        sl = ServeSlot();
+                        continue;
+                    }
+                    if (r.attempts < 8) {
+                        if (status == ST_HASH_FULL) r.mult *= 4;
+                        else r.heap_mult *= 16;
+                        if (r.large)
+                            promoted.push_front(std::move(r));
+                        else
+                            pending.insert(pending.begin(), std::move(r));
+                        sl = ServeSlot();
+                        continue;
+                    }
+                }
+                if (status == ST_OK) {
+                    const int w = walk_of[q];
+                    const uint64_t len = lens[w];
+                    const unsigned long long *kk = keys.data() + koff[w];
+                    const auto &in = r.inst;
+                    if (len > kcap[w]) {
+                        status = UASTAR_ARENA_FULL;
+                    } else if (in.kind == UASTAR_KIND_GRID) {
+                        r.acc.straight = (int64_t)(o.goal_best >> 32);
+                        r.acc.diagonal = (int64_t)(o.goal_best & 0xffffffffu);
+                        std::vector<int32_t> path(len);
+                        for (uint64_t u = 0; u < len; ++u) path[u] = (int32_t)kk[len - 1 - u];
+                        int64_t a2 = 0, b2 = 0;
+                        float fc = 0;
+                        if (uastar_validate_grid_path(r.words.data(), in.H, in.W, in.sx, in.sy, in.ex, in.ey,
+                                                      path.data(), (int64_t)len, &a2, &b2, &fc) != UASTAR_OK ||
+                            a2 != r.acc.straight || b2 != r.acc.diagonal)
+                            status = UASTAR_CUDA_ERROR;
+                        r.acc.cost = fc;
+                    } else {
+                        r.acc.steps = (int32_t)o.goal_best;
+                        std::vector<int32_t> moves;
+                        auto blank = [&](uint64_t k) {
+                            for (int c = 0; c < in.n * in.n; ++c)
+                                if (((k >> (4 * c)) & 15) == 0) return c;
+                            return -1;
+                        };
+                        for (uint64_t u = len - 1; u >= 1; --u) {
+                            const int pb = blank(kk[u]), cb = blank(kk[u - 1]);
+                            moves.push_back(cb - pb == in.n ? 0 : cb - pb == -in.n ? 1 : cb - pb == 1 ? 2 : 3);
+                        }
+                        if ((int64_t)moves.size() != r.acc.steps ||
+                            uastar_validate_puzzle_moves(in.n, in.tiles, moves.data(), (int64_t)moves.size()) !=
+                                UASTAR_OK)
+                            status = UASTAR_CUDA_ERROR;
+                    }
+                }
+                serve_complete(S, r, status);
+                sl = ServeSlot();
+            }
+            if (S->loop_error) break;
         }
+        if (S->loop_error) break;
     }
     // drain: anything left is reported as cancelled
     for (auto &r : pending) serve_complete(S, r, UASTAR_CANCELLED);
-    for (auto &sl : slots)
-        if (sl.busy) serve_complete(S, sl.req, UASTAR_CANCELLED);
+    for (auto &r : promoted) serve_complete(S, r, UASTAR_CANCELLED);
+    for (auto &t : S->tier)
+        for (auto &sl : t.slots)
+            if (sl.busy) serve_complete(S, sl.req, UASTAR_CANCELLED);
     std::deque<ServeReq> rest;
     {
         std::lock_guard<std::mutex> lk(S->mu);
         rest.swap(S->incoming);
     }
     for (auto &r : rest) serve_complete(S, r, UASTAR_CANCELLED);
+}
+
+static void serve_free(ServeState *S) {
+    for (auto &t : S->tier) {
+        for (DevBuf *b : {&t.d_descs, &t.d_outs, &t.d_states, &t.d_hsize, &t.d_cand, &t.d_walk}) b->release();
+        if (t.e0) cudaEventDestroy(t.e0);
+        if (t.e1) cudaEventDestroy(t.e1);
+        if (t.stream) cudaStreamDestroy(t.stream);
+    }
+    for (DevBuf *b : {&S->tab, &S->bitmaps, &S->heaps}) b->release();
 }
 
 }  // namespace uastar
@@ -1329,24 +1468,36 @@ int32_t uastar_serve_start(uastar_engine *eng, const uastar_serve_config *cfg) {
     S->eng = eng;
     if (cfg) S->cfg = *cfg;
     if (!(S->cfg.hbm_budget_gb > 0)) S->cfg.hbm_budget_gb = 120.0;
-    int32_t grc = resolve_block_geometry(eng, S->cfg.threads_per_instance, S->cfg.threads_per_heap, &S->geo);
+    ServeTier &small = S->tier[0], &large = S->tier[1];
+    int32_t grc = resolve_block_geometry(eng, S->cfg.threads_per_instance, S->cfg.threads_per_heap, &small.geo);
     if (grc) {
         delete S;
         return grc;
     }
-    S->T = S->geo.T;
-    S->geo.set_capacity(S->cfg.heap_capacity > 0 ? (uint64_t)S->cfg.heap_capacity : 4095);
-    const int max_slots = S->geo.ctas;
-    cudaError_t e = cudaSuccess;
-    S->S = S->cfg.slots > 0 ? std::min(S->cfg.slots, max_slots) : max_slots;
+    small.geo.set_capacity(S->cfg.heap_capacity > 0 ? (uint64_t)S->cfg.heap_capacity : 4095);
+    large.geo = small.geo;
+    large.large = true;
+    const int capacity = small.geo.ctas;  // co-resident CTAs of the quantum kernels
+    // Cluster slots: a quarter of the capacity (at least one 8-CTA cluster)
+    // unless the caller asked for fewer slots than one cluster.
+    int nlarge = 0;
+    if (resolve_cluster_geometry(eng, 8, &large.geo) == UASTAR_OK)
+        nlarge = std::max(1, std::min(large.geo.ctas / 8, capacity / 8 / 4));
+    int nsmall = capacity - 8 * nlarge;
+    if (S->cfg.slots > 0) {
+        nsmall = std::min(nsmall, S->cfg.slots);
+        if (S->cfg.slots < 8) nlarge = 0;
+    }
+    small.nslots = std::max(1, nsmall);
+    large.nslots = nlarge;
     // The budget is split into three arenas that requests draw from:
     // heap slices (20 %), grid bitmaps (5 %) and dedup partitions (75 %).
     const double budget_b = S->cfg.hbm_budget_gb * 1e9;
-    const uint64_t heap_entries = (uint64_t)(budget_b * 0.20 / 16);
+    const uint64_t heap_units = (uint64_t)(budget_b * 0.20 / 16);
     const uint64_t bm_words = (uint64_t)(budget_b * 0.05 / 8);
     const double tab_b = budget_b * 0.75;
-    S->heap_bytes = heap_entries * 16;
-    if (tab_b < (double)(1u << 20) * sizeof(Slot) || heap_entries * 16 < (uint64_t)S->geo.H * S->geo.slice) {
+    S->heap_bytes = heap_units * 16;
+    if (tab_b < (double)(1u << 20) * sizeof(Slot) || heap_units * 16 < (uint64_t)small.geo.H * small.geo.slice) {
         delete S;
         eng->set_err("serving budget too small");
         return UASTAR_BAD_INPUT;
@@ -1354,19 +1505,30 @@ int32_t uastar_serve_start(uastar_engine *eng, const uastar_serve_config *cfg) {
     const uint64_t tab_slots = (uint64_t)(tab_b / sizeof(Slot));
     S->tab_alloc.reset(tab_slots);
     S->bm_alloc.reset(bm_words);
-    S->heap_alloc.reset(heap_entries);
-    if ((e = S->tab.ensure(tab_slots * sizeof(Slot))) != cudaSuccess ||
-        (e = S->bitmaps.ensure(bm_words * 8 + 64)) != cudaSuccess ||
-        (e = S->heaps.ensure(S->heap_bytes)) != cudaSuccess ||
-        (e = S->hsize.ensure((size_t)S->S * S->geo.H * 4)) != cudaSuccess ||
-        (e = S->cand.ensure((size_t)S->S * S->geo.H * 8 * sizeof(Cand))) != cudaSuccess ||
-        (e = S->descs.ensure((size_t)S->S * sizeof(InstDesc))) != cudaSuccess ||
-        (e = S->outs.ensure((size_t)S->S * sizeof(InstOut))) != cudaSuccess ||
-        (e = S->states.ensure((size_t)S->S * sizeof(TeamState))) != cudaSuccess ||
-        (e = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking)) != cudaSuccess ||
-        (e = cudaEventCreate(&S->q0)) != cudaSuccess || (e = cudaEventCreate(&S->q1)) != cudaSuccess) {
-        for (DevBuf *b : {&S->tab, &S->bitmaps, &S->heaps, &S->hsize, &S->cand, &S->descs, &S->outs, &S->states})
-            b->release();
+    S->heap_alloc.reset(heap_units);
+    cudaError_t e = cudaSuccess;
+    if ((e = S->tab.ensure(tab_slots * sizeof(Slot))) == cudaSuccess)
+        e = S->bitmaps.ensure(bm_words * 8 + 64);
+    if (e == cudaSuccess) e = S->heaps.ensure(S->heap_bytes);
+    for (auto &t : S->tier) {
+        if (e != cudaSuccess) break;
+        const size_t ctas = (size_t)t.nslots * (t.large ? 8 : 1);
+        t.slots.assign(t.nslots, ServeSlot());
+        t.descs.assign(t.nslots, InstDesc());
+        std::memset(t.descs.data(), 0, t.descs.size() * sizeof(InstDesc));
+        t.outs.assign(t.nslots, InstOut());
+        if (!t.nslots) continue;
+        if ((e = t.d_descs.ensure((size_t)t.nslots * sizeof(InstDesc))) != cudaSuccess ||
+            (e = t.d_outs.ensure((size_t)t.nslots * sizeof(InstOut))) != cudaSuccess ||
+            (e = t.d_states.ensure((size_t)t.nslots * sizeof(TeamState))) != cudaSuccess ||
+            (e = t.d_hsize.ensure(ctas * t.geo.H * 4)) != cudaSuccess ||
+            (e = t.d_cand.ensure(ctas * t.geo.H * 8 * sizeof(Cand))) != cudaSuccess ||
+            (e = cudaStreamCreateWithFlags(&t.stream, cudaStreamNonBlocking)) != cudaSuccess ||
+            (e = cudaEventCreate(&t.e0)) != cudaSuccess || (e = cudaEventCreate(&t.e1)) != cudaSuccess)
+            break;
+    }
+    if (e != cudaSuccess) {
+        serve_free(S);
         delete S;
         return fail_cuda(eng, e, "serving allocation");
     }
@@ -1472,13 +1634,9 @@ int32_t uastar_serve_stop(uastar_engine *eng, double timeout_s, uastar_serve_sta
     if (S->th.joinable()) S->th.join();
     const int32_t rc = S->loop_error;
     if (stats) *stats = S->stats;
-    cudaStreamSynchronize(S->stream);
-    for (DevBuf *b : {&S->tab, &S->bitmaps, &S->heaps, &S->hsize, &S->cand, &S->descs, &S->outs, &S->states,
-                      &S->walk})
-        b->release();
-    cudaEventDestroy(S->q0);
-    cudaEventDestroy(S->q1);
-    cudaStreamDestroy(S->stream);
+    for (auto &t : S->tier)
+        if (t.stream) cudaStreamSynchronize(t.stream);
+    serve_free(S);
     delete S;
     eng->serve = nullptr;
     return rc;
