@@ -57,14 +57,15 @@ enum {
 typedef struct uastar_engine uastar_engine;
 
 typedef struct {
-    int32_t heaps;           /* k parallel binary heaps of the plain engine (0 -> 8192) */
+    int32_t heaps;           /* k parallel binary heaps of the plain engine (0 -> 8192 grid, 16384 puzzle) */
     int32_t block_threads;   /* CTA size of the plain engine's persistent kernel (0 -> 256) */
     int32_t heap_capacity;   /* entries per heap (0 -> auto, grown on overflow) */
-    int32_t hash_log2_slots; /* dedup table = 2^n slots of 32 B (0 -> auto from instance) */
+    int32_t hash_log2_slots; /* dedup table = 2^n slots of 32 B (0 -> sized from the instance and
+                              grown 4x in place whenever it is half full) */
     double max_load;         /* dedup table load limit in (0,1) (0 -> 0.8) */
     int64_t max_rounds;      /* GA* round limit per solve (0 -> 2^31) */
     double wait_timeout_s;   /* bound on any device-side barrier wait (0 -> 10 s) */
-    int32_t threads_per_heap; /* threads that share one heap's successors (0 -> 4 grid, 2 puzzle) */
+    int32_t threads_per_heap; /* threads that share one heap's successors (0 -> 4) */
     int32_t heap_top_levels;  /* heap levels kept in shared memory (0 -> as many as fit, -1 -> none) */
 } uastar_config;
 
@@ -87,7 +88,7 @@ const char *uastar_build_info(void);
 /* ---- grid pathfinding (--pathway) ------------------------------------- */
 typedef struct {
     int32_t status;
-    int32_t reserved;
+    int32_t table_grows;  /* times the auto-sized dedup table grew in place */
     int64_t straight;     /* exact optimal cost = straight + diagonal*sqrt(2) */
     int64_t diagonal;
     float cost;           /* float32 g accumulated along the path in order, as the
@@ -132,6 +133,8 @@ typedef struct {
     int64_t table_used;
     double kernel_ms;
     double solve_ms;
+    int32_t table_grows;  /* times the auto-sized dedup table grew in place */
+    int32_t reserved;
 } uastar_puzzle_result;
 
 /* Build the disjoint pattern databases of the n x n puzzle on the GPU by
@@ -189,7 +192,7 @@ typedef struct {
 
 typedef struct {
     int32_t threads_per_instance; /* CTA size per instance (0 -> 256) */
-    int32_t threads_per_heap;     /* heaps per instance = threads_per_instance / this (0 -> 1) */
+    int32_t threads_per_heap;     /* heaps per instance = threads_per_instance / this (0 -> 4) */
     int32_t heap_capacity;        /* entries per heap (0 -> autotuned) */
     double load_factor;           /* target dedup-partition load (0 -> autotuned) */
     int32_t ctas;                 /* persistent CTAs (0 -> all SMs x occupancy) */

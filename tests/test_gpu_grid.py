@@ -107,12 +107,14 @@ def test_small_fixed_table_reports_hash_full():
 
 
 def test_auto_table_grows_on_overflow():
-    # auto-sized tables grow and retry; the result is unchanged
-    sp = WL.screened_grid(300, 300, 0.2, 1, exact=True)
+    # the auto-sized table of the 1000^2 grid starts at 2^20 slots and is
+    # moved to a 4x table in place when half full; the result is unchanged
+    c = golden("grid_c1.json")
+    w = case_words(c)
     with Engine(0) as eng:
-        r = eng.grid_solve(sp.words(), 300, 300, sp.start, sp.goal)
-        ex = O.grid_astar_exact(sp.words(), 300, 300, sp.start, sp.goal)
-        assert r.ok and (r.straight, r.diagonal) == (ex.straight, ex.diagonal)
+        r = eng.grid_solve(w, c["H"], c["W"], tuple(c["start"]), tuple(c["goal"]))
+        assert r.table_grows >= 1 and r.table_used > (1 << 19)
+        check_against(r, eng.grid_path(), w, c)
 
 
 def test_small_fixed_heaps_report_overflow():

@@ -113,3 +113,16 @@ def test_missing_pdb_is_reported():
     with Engine(0) as e:
         with pytest.raises(EngineError):
             e.puzzle_solve(3, [8, 1, 3, 4, 0, 2, 7, 6, 5])
+
+
+def test_table_grows_in_place_hard_puzzle(peng):
+    """A hard 15-puzzle (63 moves, ~4e7 expansions) outgrows the auto-sized
+    2^22-slot starting table several times; the paused search is moved to a
+    4x table each time and resumed, and still returns the reference's optimum."""
+    row = golden("mixed_c4.json")[127]
+    tiles = E.gen_puzzle(row["seed"], 4, row["walk"])
+    r = peng.puzzle_solve(4, tiles)
+    assert r.ok and r.steps == row["ref"]["steps"] == 63
+    assert r.table_grows >= 2
+    assert r.table_used > (1 << 22)
+    assert E.validate_puzzle_moves(4, tiles, peng.puzzle_moves())

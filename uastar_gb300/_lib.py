@@ -31,7 +31,7 @@ class Config(C.Structure):
 
 
 class GridResult(C.Structure):
-    _fields_ = [("status", C.c_int32), ("reserved", C.c_int32), ("straight", C.c_int64),
+    _fields_ = [("status", C.c_int32), ("table_grows", C.c_int32), ("straight", C.c_int64),
                 ("diagonal", C.c_int64), ("cost", C.c_float), ("pad", C.c_float),
                 ("cost_exact", C.c_double), ("expanded", C.c_int64), ("generated", C.c_int64),
                 ("pushed", C.c_int64), ("rounds", C.c_int64), ("table_used", C.c_int64),
@@ -41,7 +41,8 @@ class GridResult(C.Structure):
 class PuzzleResult(C.Structure):
     _fields_ = [("status", C.c_int32), ("steps", C.c_int32), ("expanded", C.c_int64),
                 ("generated", C.c_int64), ("pushed", C.c_int64), ("rounds", C.c_int64),
-                ("table_used", C.c_int64), ("kernel_ms", C.c_double), ("solve_ms", C.c_double)]
+                ("table_used", C.c_int64), ("kernel_ms", C.c_double), ("solve_ms", C.c_double),
+                ("table_grows", C.c_int32), ("reserved", C.c_int32)]
 
 
 class Instance(C.Structure):

@@ -47,12 +47,16 @@ struct InstDesc {
     uint64_t heap_off;    // serving: byte offset of this request's heap slice
     uint32_t heap_stride; // serving: entries per heap of that slice
     uint32_t heap_hcap;   // serving: maximum heap size
+    uint64_t budget;      // batch: rounds before the instance gives up its team (0: the launch's)
+    uint64_t key_off;     // batch: first path key of this instance in the key buffer
+    uint64_t key_cap;     // batch: room for path keys
 };
 
 struct InstOut {
     uint32_t status, goal_slot;
     unsigned long long goal_best, rounds, expanded, generated, pushed, inserted;
     unsigned long long t_start, t_end;  // device globaltimer around this call's work (ns)
+    unsigned long long path_len;        // batch: keys written (goal -> start); key_cap + 1 if cut
 };
 
 struct BatchArgs {
@@ -66,7 +70,7 @@ struct BatchArgs {
     uint8_t *heaps;        // per CTA: H heaps x slice bytes
     uint64_t slice;        // bytes per heap (batch)
     uint32_t *hsize;       // per CTA: H
-    Cand *cand;            // per CTA: H * 8
+    Cand *cand;            // per CTA: 2 * H * 8 (two rounds)
     uint32_t H;            // heaps per instance (CTA)
     uint32_t L_grid, L_puzzle;            // heap levels in shared memory
     uint32_t stride_grid, stride_puzzle;  // batch heap geometry per entry type
@@ -78,7 +82,23 @@ struct BatchArgs {
     double max_load;
     uint64_t budget;       // rounds per call (serving quantum) or ~0
     int serving;           // 1: CTA b serves slot b; 0: work queue
+    uint64_t region_slots; // batch: dedup region of each team (reused by the instances it takes)
+    unsigned long long *keys;  // batch: path keys of solved instances
 };
+
+// Writes the keys of the prev chain from `goal_slot` (goal -> start) and
+// returns their number, or cap + 1 if the chain is longer than cap.  One
+// thread: a pointer chase.
+__device__ unsigned long long walk_chain(const Slot *part, uint32_t goal_slot, unsigned long long *out,
+                                         uint64_t cap) {
+    uint32_t s = goal_slot;
+    uint64_t n = 0;
+    while (s != kNone && n < cap) {
+        out[n++] = __ldcg(&part[s].key);
+        s = __ldcg(&part[s].prev);
+    }
+    return s != kNone ? cap + 1 : n;
+}
 
 __device__ void clear_partition(Slot *tab, uint64_t slots) {
     uint4 *p = reinterpret_cast<uint4 *>(tab);
@@ -86,19 +106,12 @@ __device__ void clear_partition(Slot *tab, uint64_t slots) {
     for (uint64_t j = threadIdx.x; j < slots * 2; j += blockDim.x) p[j] = v;
 }
 
-__device__ void init_state(TeamState *st) {
-    memset(st, 0, sizeof(TeamState));
-    st->round_min[0] = st->round_min[1] = kInfCost;
-    st->goal_best = kInfCost;
-    st->goal_slot = kNone;
-    st->status = ST_RUNNING;
-}
+__device__ void init_state(TeamState *st) { team_state_init(st); }
 
 // Runs one instance on this CTA for up to `budget` rounds.
 template <class Team>
-__device__ uint32_t run_instance(const BatchArgs &a, const InstDesc &d, Team &team, uint8_t *heaps,
+__device__ uint32_t run_instance(const BatchArgs &a, const InstDesc &d, Team &team, Slot *tab, uint8_t *heaps,
                                  uint32_t *hs, Cand *cand, unsigned char *smem, uint64_t budget) {
-    Slot *tab = a.tab + d.tab_off;
     const uint64_t slots = 1ull << d.log2_slots;
     const bool own_geo = a.serving != 0;  // serving requests carry their heap geometry
     if (d.kind == UASTAR_KIND_GRID) {
@@ -143,7 +156,7 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
     // serving: each request owns a slice named by its descriptor
     uint8_t *heaps = a.heaps + (size_t)blockIdx.x * H * a.slice;
     uint32_t *hs = a.hsize + (size_t)blockIdx.x * H;
-    Cand *cand = a.cand + (size_t)blockIdx.x * H * 8;
+    Cand *cand = a.cand + (size_t)blockIdx.x * H * 16;
     for (uint32_t iter = 0;; ++iter) {
         if (a.serving) {
             if (iter > 0 || blockIdx.x >= a.count) break;
@@ -158,9 +171,11 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
         if (a.serving && d.kind == 0) break;  // empty serving slot
         const unsigned long long t_start = globaltimer_ns();
         if (a.serving) heaps = a.heaps + d.heap_off;
+        // serving: the request's own partition; batch: this CTA's region
+        Slot *const tab = a.serving ? a.tab + d.tab_off : a.tab + (size_t)blockIdx.x * a.region_slots;
         if (!a.serving || d.fresh) {
             // serving partitions are cleared by the host at admission (fresh == 2)
-            if (d.fresh != 2) clear_partition(a.tab + d.tab_off, 1ull << d.log2_slots);
+            if (d.fresh != 2) clear_partition(tab, 1ull << d.log2_slots);
             for (uint32_t j = threadIdx.x; j < H; j += blockDim.x) hs[j] = 0;
             if (threadIdx.x == 0) init_state(&st);
         } else if (threadIdx.x == 0) {
@@ -168,10 +183,11 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
         }
         __syncthreads();
         BlockTeam team{&st};
-        run_instance(a, d, team, heaps, hs, cand, smem, a.budget);
+        run_instance(a, d, team, tab, heaps, hs, cand, smem, d.budget ? d.budget : a.budget);
         __syncthreads();
         if (threadIdx.x == 0) {
             InstOut o;
+            o.path_len = 0;
             o.status = st.status;
             o.goal_slot = st.goal_slot;
             o.goal_best = st.goal_best;
@@ -183,8 +199,11 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
             o.t_start = t_start;
             o.t_end = globaltimer_ns();
             // a phase-2 error of the last round of a quantum is still in error2
-            if (o.status == ST_RUNNING && (st.error || st.error2[0] || st.error2[1]))
-                o.status = st.error ? st.error : (st.error2[0] ? st.error2[0] : st.error2[1]);
+            const uint32_t pend = team_state_pending_error(st.error, st.err2);
+            if (o.status == ST_RUNNING && pend) o.status = pend;
+            // batch: the region is reused by the next instance, so the path
+            // is read out now
+            if (!a.serving && o.status == ST_OK) o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap);
             a.outs[i] = o;
             if (a.serving) a.states[i] = st;
         }
@@ -211,7 +230,7 @@ __global__ void __launch_bounds__(512, 1) k_batch_cluster(BatchArgs a) {
     ClusterTeam team{st};
     uint8_t *heaps = a.heaps + (size_t)cid * csize * H * a.slice;
     uint32_t *hs = a.hsize + (size_t)cid * csize * H;
-    Cand *cand = a.cand + (size_t)cid * csize * H * 8;
+    Cand *cand = a.cand + (size_t)cid * csize * H * 16;
     for (uint32_t iter = 0;; ++iter) {
         uint32_t i;
         if (a.serving) {
@@ -228,17 +247,19 @@ __global__ void __launch_bounds__(512, 1) k_batch_cluster(BatchArgs a) {
         if (a.serving && d.kind == 0) break;  // empty slot
         if (a.serving) heaps = a.heaps + d.heap_off;
         const unsigned long long t_start = globaltimer_ns();
+        Slot *const tab = a.serving ? a.tab + d.tab_off : a.tab + (size_t)cid * a.region_slots;
         if (!a.serving || d.fresh) {
             // serving partitions are cleared by the host at admission (fresh == 2)
-            if (d.fresh != 2) clear_partition_team(a.tab + d.tab_off, 1ull << d.log2_slots, crank, csize);
+            if (d.fresh != 2) clear_partition_team(tab, 1ull << d.log2_slots, crank, csize);
             for (uint32_t j = threadIdx.x; j < H; j += blockDim.x) hs[crank * H + j] = 0;
             if (crank == 0 && threadIdx.x == 0) init_state(st);
         }
         team.sync();
-        run_instance(a, d, team, heaps, hs, cand, smem, a.budget);
+        run_instance(a, d, team, tab, heaps, hs, cand, smem, d.budget ? d.budget : a.budget);
         team.sync();
         if (crank == 0 && threadIdx.x == 0) {
             InstOut o;
+            o.path_len = 0;
             o.status = ldcg_u32(&st->status);
             o.goal_slot = ldcg_u32(&st->goal_slot);
             o.goal_best = ldcg_u64(&st->goal_best);
@@ -249,8 +270,10 @@ __global__ void __launch_bounds__(512, 1) k_batch_cluster(BatchArgs a) {
             o.inserted = ldcg_u64(&st->inserted);
             o.t_start = t_start;
             o.t_end = globaltimer_ns();
-            const uint32_t e1 = ldcg_u32(&st->error), e20 = ldcg_u32(&st->error2[0]), e21 = ldcg_u32(&st->error2[1]);
-            if (o.status == ST_RUNNING && (e1 || e20 || e21)) o.status = e1 ? e1 : (e20 ? e20 : e21);
+            const uint32_t e2[3] = {ldcg_u32(&st->err2[0]), ldcg_u32(&st->err2[1]), ldcg_u32(&st->err2[2])};
+            const uint32_t pend = team_state_pending_error(ldcg_u32(&st->error), e2);
+            if (o.status == ST_RUNNING && pend) o.status = pend;
+            if (!a.serving && o.status == ST_OK) o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap);
             a.outs[i] = o;
         }
         team.sync();
@@ -264,16 +287,7 @@ __global__ void k_batch_walk(const InstDesc *descs, const InstOut *outs, const u
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nwhich) return;
     const uint32_t i = which[t];
-    const Slot *part = tab + descs[i].tab_off;
-    uint32_t s = outs[i].goal_slot;
-    const uint64_t cap = key_cap[t];
-    unsigned long long *out = keys + key_off[t];
-    uint64_t n = 0;
-    while (s != kNone && n < cap) {
-        out[n++] = __ldcg(&part[s].key);
-        s = __ldcg(&part[s].prev);
-    }
-    lens[t] = (s != kNone) ? cap + 1 : n;
+    lens[t] = walk_chain(tab + descs[i].tab_off, outs[i].goal_slot, keys + key_off[t], key_cap[t]);
 }
 
 }  // namespace uastar
@@ -329,11 +343,13 @@ bool board_solvable(int n, const uint8_t *tiles) {
 uint64_t est_nodes(const uastar_instance &in) {
     if (in.est_nodes > 0) return (uint64_t)in.est_nodes;
     // Grids: an eighth of the cells (random grids searched corner to corner
-    // touch a few percent to ~20 %).  Puzzles: 2^17 states (the median 15-puzzle
-    // of 60-300 random moves needs ~2e5 expansions).  An instance that fills
-    // its partition is re-run in the next wave with 16x the space.
+    // touch a few percent to ~20 %).  15-puzzles: 2^19 states, what a single
+    // CTA team inserts in its 4096-round budget (64 heaps, ~2 new states per
+    // expansion), so that a puzzle leaves that tier by running out of rounds
+    // rather than out of space.  An instance that fills its partition is
+    // re-run in the next wave with 16x the space.
     if (in.kind == UASTAR_KIND_GRID) return std::max<uint64_t>(4096, (uint64_t)in.H * in.W / 8);
-    return in.n == 3 ? 65536 : 262144;
+    return in.n == 3 ? 65536 : 524288;
 }
 
 struct BatchPlan {
@@ -395,7 +411,7 @@ template <class P> uint32_t fit_top(uint32_t H, size_t budget) {
 int32_t resolve_block_geometry(uastar_engine *eng, int threads, int tph, BatchGeometry *g) {
     g->T = threads > 0 ? threads : 256;
     g->T = std::max(32, std::min(512, (g->T + 31) / 32 * 32));
-    tph = std::max(1, std::min(tph > 0 ? tph : 1, g->T));
+    tph = std::max(1, std::min(tph > 0 ? tph : 4, g->T));
     g->H = (uint32_t)std::max(1, g->T / tph);
     int smem_sm = 0;
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, eng->device);
@@ -453,9 +469,14 @@ int32_t resolve_geometry(uastar_engine *eng, const uastar_batch_config *cfg, Bat
 }
 
 // Runs `idx` (indices into insts) as one wave; fills results for them.
+// Each team (CTA or cluster) owns one dedup region, sized for the largest
+// partition of the wave and reused by every instance the team takes, so the
+// wave's table memory is teams x region, not the sum over instances.
+// `puzzle_budget` (0: none) is a round budget for puzzle instances only.
 int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::vector<int> &idx,
                  const BatchGeometry &g, const std::vector<int> &space_mult, bool use_graph, uint64_t budget,
-                 uastar_instance_result *results, uastar_batch_stats *stats, std::vector<int> *retry) {
+                 uint64_t puzzle_budget, uastar_instance_result *results, uastar_batch_stats *stats,
+                 std::vector<int> *retry) {
     cudaError_t e;
     const int cnt = (int)idx.size();
     // plan: order largest estimate first (longest-processing-time first)
@@ -467,7 +488,7 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
 
     std::vector<InstDesc> descs(cnt);
     std::vector<int> slot_of(cnt);  // position of wave instance j in descs
-    uint64_t bm_words = 0, tab_slots = 0;
+    uint64_t bm_words = 0, region_slots = 1u << 12, ktot = 0;
     for (int p = 0; p < cnt; ++p) {
         const int j = order[p];
         const uastar_instance &in = insts[idx[j]];
@@ -479,8 +500,12 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
         uint64_t slots = next_pow2_u64((uint64_t)((double)est[j] / g.load));
         slots = std::max<uint64_t>(slots, 1u << 12);
         d.log2_slots = (uint32_t)log2_u64(slots);
-        d.tab_off = tab_slots;
-        tab_slots += slots;
+        region_slots = std::max(region_slots, slots);
+        // path keys: a longer path (a maze) goes to the plain engine
+        d.key_off = ktot;
+        d.key_cap = in.kind == UASTAR_KIND_GRID ? 2ull * ((uint64_t)in.H + in.W) + 64 : 256;
+        ktot += d.key_cap;
+        d.budget = in.kind == UASTAR_KIND_PUZZLE ? puzzle_budget : 0;
         if (in.kind == UASTAR_KIND_GRID) {
             d.H = in.H;
             d.W = in.W;
@@ -497,24 +522,27 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
         slot_of[j] = p;
     }
     // device buffers
-    const size_t tab_b = tab_slots * sizeof(Slot);
+    const int teams = g.csize > 0 ? std::min(g.ctas / g.csize, cnt) : std::min(g.ctas, cnt);
+    const size_t tab_b = (size_t)teams * region_slots * sizeof(Slot);
     const size_t heap_b = (size_t)g.ctas * g.H * g.slice;
     if (debug_log())
-        std::fprintf(stderr, "[uastar] wave: %d instances, %s teams of %d CTAs x %d threads, %d heaps each, "
-                             "budget %llu rounds, partitions %.2f GB, heap slices %.2f GB (%llu B/heap)\n",
-                     cnt, g.csize > 0 ? "cluster" : "CTA", g.csize > 0 ? g.csize : 1, g.T, (int)g.H,
-                     (unsigned long long)budget, tab_slots * 32.0 / 1e9, heap_b / 1e9,
-                     (unsigned long long)g.slice);
+        std::fprintf(stderr, "[uastar] wave: %d instances, %d %s teams of %d CTAs x %d threads, %d heaps each, "
+                             "budget %llu rounds (puzzles %llu), regions %.2f GB (2^%d slots each), heap slices "
+                             "%.2f GB (%llu B/heap)\n",
+                     cnt, teams, g.csize > 0 ? "cluster" : "CTA", g.csize > 0 ? g.csize : 1, g.T, (int)g.H,
+                     (unsigned long long)budget, (unsigned long long)puzzle_budget, tab_b / 1e9,
+                     (int)log2_u64(region_slots), heap_b / 1e9, (unsigned long long)g.slice);
     if ((e = eng->b_tab.ensure(tab_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc partitions");
     if ((e = eng->b_heaps.ensure(heap_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc heap slices");
     if ((e = eng->b_hsize.ensure((size_t)g.ctas * g.H * 4)) != cudaSuccess) return fail_cuda(eng, e, "alloc");
-    if ((e = eng->b_cand.ensure((size_t)g.ctas * g.H * 8 * sizeof(Cand))) != cudaSuccess)
+    if ((e = eng->b_cand.ensure((size_t)g.ctas * g.H * 16 * sizeof(Cand))) != cudaSuccess)
         return fail_cuda(eng, e, "alloc");
     if ((e = eng->b_desc.ensure(cnt * sizeof(InstDesc))) != cudaSuccess) return fail_cuda(eng, e, "alloc");
     if ((e = eng->b_out.ensure(cnt * sizeof(InstOut))) != cudaSuccess) return fail_cuda(eng, e, "alloc");
     if ((e = eng->b_queue.ensure(64)) != cudaSuccess) return fail_cuda(eng, e, "alloc");
     if ((e = eng->b_bitmaps.ensure(std::max<size_t>(16, bm_words * 8))) != cudaSuccess)
         return fail_cuda(eng, e, "alloc bitmaps");
+    if ((e = eng->b_walk.ensure(std::max<size_t>(64, ktot * 8))) != cudaSuccess) return fail_cuda(eng, e, "alloc keys");
     // bitmaps H2D (one copy per grid)
     for (int p = 0; p < cnt; ++p) {
         const int j = order[p];
@@ -554,6 +582,8 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
     a.hcap_grid = g.hg_grid.hcap;
     a.hcap_puzzle = g.hg_puzzle.hcap;
     a.budget = budget;
+    a.region_slots = region_slots;
+    a.keys = eng->b_walk.as<unsigned long long>();
     int ctas = std::min(g.ctas, cnt);
     cudaLaunchConfig_t lc = {};
     cudaLaunchAttribute lat[1];
@@ -629,43 +659,12 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
         std::fprintf(stderr, "\n");
     }
 
-    // paths of solved instances: one walker thread each
-    std::vector<uint32_t> which;
-    std::vector<uint64_t> koff, kcap;
-    uint64_t ktot = 0;
-    for (int p = 0; p < cnt; ++p) {
-        if (outs[p].status != ST_OK) continue;
-        const uastar_instance &in = insts[idx[order[p]]];
-        const uint64_t cap = in.kind == UASTAR_KIND_GRID ? 8ull * (in.H + in.W) + 64 : 512;
-        which.push_back((uint32_t)p);
-        koff.push_back(ktot);
-        kcap.push_back(cap);
-        ktot += cap;
-    }
-    std::vector<unsigned long long> keys(ktot), lens(which.size());
-    if (!which.empty()) {
-        const size_t nw = which.size();
-        const size_t need = ktot * 8 + nw * (4 + 8 + 8 + 8) + 256;
-        if ((e = eng->b_walk.ensure(need)) != cudaSuccess) return fail_cuda(eng, e, "alloc walk");
-        char *base = eng->b_walk.as<char>();
-        unsigned long long *d_keys = reinterpret_cast<unsigned long long *>(base);
-        uint64_t *d_off = reinterpret_cast<uint64_t *>(base + ktot * 8);
-        uint64_t *d_cap = d_off + nw;
-        unsigned long long *d_len = reinterpret_cast<unsigned long long *>(d_cap + nw);
-        uint32_t *d_which = reinterpret_cast<uint32_t *>(d_len + nw);
-        cudaMemcpyAsync(d_off, koff.data(), nw * 8, cudaMemcpyHostToDevice, eng->stream);
-        cudaMemcpyAsync(d_cap, kcap.data(), nw * 8, cudaMemcpyHostToDevice, eng->stream);
-        cudaMemcpyAsync(d_which, which.data(), nw * 4, cudaMemcpyHostToDevice, eng->stream);
-        k_batch_walk<<<(unsigned)((nw + 127) / 128), 128, 0, eng->stream>>>(
-            eng->b_desc.as<InstDesc>(), eng->b_out.as<InstOut>(), d_which, (uint32_t)nw, eng->b_tab.as<Slot>(),
-            d_keys, d_off, d_cap, d_len);
-        eng->launches++;
-        cudaMemcpyAsync(lens.data(), d_len, nw * 8, cudaMemcpyDeviceToHost, eng->stream);
-        cudaMemcpyAsync(keys.data(), d_keys, ktot * 8, cudaMemcpyDeviceToHost, eng->stream);
-        if ((e = cudaStreamSynchronize(eng->stream)) != cudaSuccess) return fail_cuda(eng, e, "batch walk");
-    }
-    std::vector<int> walk_of(cnt, -1);
-    for (size_t w = 0; w < which.size(); ++w) walk_of[which[w]] = (int)w;
+    // paths of solved instances, walked by their teams (goal -> start)
+    std::vector<unsigned long long> keys(ktot);
+    if (ktot && (e = cudaMemcpyAsync(keys.data(), eng->b_walk.p, ktot * 8, cudaMemcpyDeviceToHost, eng->stream)) !=
+                    cudaSuccess)
+        return fail_cuda(eng, e, "path keys");
+    if ((e = cudaStreamSynchronize(eng->stream)) != cudaSuccess) return fail_cuda(eng, e, "path keys");
     unsigned long long t_first = ~0ull;
     for (int p = 0; p < cnt; ++p) t_first = std::min(t_first, outs[p].t_start);
 
@@ -685,19 +684,20 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
             stats->expanded += (int64_t)o.expanded;
             stats->generated += (int64_t)o.generated;
         }
-        if ((o.status == ST_HASH_FULL || o.status == ST_HEAP_OVERFLOW || o.status == ST_RUNNING) && retry) {
+        const bool long_path = o.status == ST_OK && o.path_len > descs[p].key_cap;
+        if ((o.status == ST_HASH_FULL || o.status == ST_HEAP_OVERFLOW || o.status == ST_RUNNING || long_path) &&
+            retry) {
             retry->push_back(idx[j]);
             continue;
         }
         if (o.status != ST_OK) continue;
-        const int w = walk_of[p];
-        const uint64_t len = lens[w];
-        if (len > kcap[w]) {
+        const uint64_t len = o.path_len;
+        if (long_path) {
             r.status = UASTAR_ARENA_FULL;
             continue;
         }
         // keys are goal -> start
-        const unsigned long long *kk = keys.data() + koff[w];
+        const unsigned long long *kk = keys.data() + descs[p].key_off;
         if (in.kind == UASTAR_KIND_GRID) {
             r.straight = (int64_t)(o.goal_best >> 32);
             r.diagonal = (int64_t)(o.goal_best & 0xffffffffu);
@@ -779,7 +779,8 @@ int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int
     // that an unexpectedly large one moves on instead of holding a CTA),
     // cluster teams of 8 CTAs for large grids, for instances that ran out of
     // rounds and for those that overflowed (with 16x the space); whatever
-    // overflows a cluster team goes to the plain engine (the whole GPU).
+    // overflows a cluster team or outlasts its round budget goes to the plain
+    // engine (the whole GPU).
     std::vector<int> mult(count, 1);
     const bool use_graph = !cfg || cfg->use_graph != 0 || cfg->threads_per_instance == 0;
     const uint64_t big_cells = 2048ull * 2048ull;
@@ -793,7 +794,7 @@ int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int
     }
     if (!tier1.empty()) {
         std::vector<int> m(tier1.size(), 1);
-        rc = run_wave(eng, insts, tier1, g, m, use_graph, 4096, results, stats, &retry);
+        rc = run_wave(eng, insts, tier1, g, m, use_graph, 4096, 0, results, stats, &retry);
         if (rc) return rc;
         // running out of rounds proves an instance large just as an overflow does
         for (int i : retry) {
@@ -812,7 +813,11 @@ int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int
         std::vector<int> m(tier2.size());
         for (size_t j = 0; j < tier2.size(); ++j) m[j] = mult[tier2[j]] * 2;
         retry.clear();
-        rc = run_wave(eng, insts, tier2, gc, m, use_graph, ~0ull, results, stats, &retry);
+        // Puzzles get a round budget here too: one that needs more is better
+        // off with the whole GPU than holding a cluster for the batch's tail.
+        // Grids do not: their rounds are bounded by the path length, which
+        // costs a cluster no more rounds than the whole GPU.
+        rc = run_wave(eng, insts, tier2, gc, m, use_graph, ~0ull, 8192, results, stats, &retry);
         if (rc) return rc;
         todo = retry;
     }
@@ -871,7 +876,7 @@ int32_t uastar_autotune(uastar_engine *eng, const uastar_instance *sample, int32
                         uastar_batch_config *best) {
     if (!eng || !sample || count <= 0 || !best) return UASTAR_BAD_INPUT;
     const int Ts[] = {128, 256, 512};
-    const int tphs[] = {1, 2};
+    const int tphs[] = {2, 4};
     const int caps[] = {2048};
     const double loads[] = {0.35, 0.6};
     std::vector<uastar_instance_result> res(count);
@@ -1522,7 +1527,7 @@ int32_t uastar_serve_start(uastar_engine *eng, const uastar_serve_config *cfg) {
             (e = t.d_outs.ensure((size_t)t.nslots * sizeof(InstOut))) != cudaSuccess ||
             (e = t.d_states.ensure((size_t)t.nslots * sizeof(TeamState))) != cudaSuccess ||
             (e = t.d_hsize.ensure(ctas * t.geo.H * 4)) != cudaSuccess ||
-            (e = t.d_cand.ensure(ctas * t.geo.H * 8 * sizeof(Cand))) != cudaSuccess ||
+            (e = t.d_cand.ensure(ctas * t.geo.H * 16 * sizeof(Cand))) != cudaSuccess ||
             (e = cudaStreamCreateWithFlags(&t.stream, cudaStreamNonBlocking)) != cudaSuccess ||
             (e = cudaEventCreate(&t.e0)) != cudaSuccess || (e = cudaEventCreate(&t.e1)) != cudaSuccess)
             break;

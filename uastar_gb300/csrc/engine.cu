@@ -35,6 +35,68 @@ __global__ void __launch_bounds__(512, 1) k_plain_search(P prob, SearchMem<typen
     ga_search<P>(prob, team, m, H, smem, ~0ull);
 }
 
+// ---- moving a paused search to a larger dedup table ----------------------
+// A paused search (ga_search returned ST_RUNNING at a round boundary) names
+// slots in three places: the slots' prev links, the heap entries and the
+// team's goal slot.  Growth re-inserts every occupied slot into the empty
+// larger table, recording old -> new in `map`, then rewrites all three.
+
+// Re-insert the occupied slots of `src` (n slots) into `dst` (mask + 1
+// empty slots).  Keys are unique, so an insert only races other keys for an
+// empty slot; prev is copied as is and rewritten by k_grow_links.
+__global__ void k_grow_move(const Slot *src, uint64_t n, Slot *dst, uint64_t mask, uint32_t *map) {
+    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 a = __ldcg(reinterpret_cast<const uint4 *>(src + s));
+        const unsigned long long key = ((unsigned long long)a.y << 32) | a.x;
+        if (key == kEmptyKey) continue;
+        const uint4 b = __ldcg(reinterpret_cast<const uint4 *>(src + s) + 1);
+        uint64_t h = mix64(key) & mask;
+        for (uint64_t probe = 0; probe <= mask; ++probe) {
+            if (atomicCAS(&dst[h].key, kEmptyKey, key) == kEmptyKey) break;
+            h = (h + 1) & mask;
+        }
+        uint4 *d = reinterpret_cast<uint4 *>(dst + h);
+        d[0] = make_uint4(a.x, a.y, a.z, a.w);  // key, g
+        d[1] = b;                               // aux, prev (old index), pad
+        map[s] = (uint32_t)h;
+    }
+}
+
+__global__ void k_grow_links(const Slot *src, uint64_t n, Slot *dst, const uint32_t *map) {
+    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
+        if (__ldcg(&src[s].key) == kEmptyKey) continue;
+        const uint32_t p = __ldcg(&src[s].prev);
+        dst[map[s]].prev = p == kNone ? kNone : map[p];
+    }
+}
+
+// One warp per heap: entries 1..size, the saved shared top first (heap
+// indices <= 2^L - 1 at the head of the heap's block), then the bricks.
+template <class P>
+__global__ void k_grow_heaps(typename P::Entry *heaps, uint32_t stride, uint32_t L, const uint32_t *heap_size,
+                             uint32_t k, const uint32_t *map, TeamState *st) {
+    using E = typename P::Entry;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t topn = (1u << L) - 1u;
+    for (uint32_t h = warp; h < k; h += nwarps) {
+        E *gblock = heaps + (size_t)h * stride;
+        const BrickHeap<P> bh{gblock + top_reserve<P>(L), nullptr, nullptr, L};
+        const uint32_t sz = heap_size[h];
+        for (uint32_t i = 1 + lane; i <= sz; i += 32) {
+            E *q = i <= topn ? gblock + i : bh.g + bh.off(i);
+            E e = P::load(q);
+            e.slot = map[e.slot];
+            P::store(q, e);
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (st->goal_slot != kNone) st->goal_slot = map[st->goal_slot];
+        st->barrier = 0;  // the next launch counts barriers from zero
+    }
+}
+
 // Walk the prev chain from the goal slot (one thread: a pointer chase).
 // Writes keys goal -> start; *len = count, or cap + 1 when truncated.
 __global__ void k_walk(const Slot *tab, uint32_t goal_slot, unsigned long long *keys,
@@ -85,11 +147,7 @@ inline double now_ms() {
 
 TeamState fresh_team_state() {
     TeamState s;
-    std::memset(&s, 0, sizeof s);
-    s.round_min[0] = s.round_min[1] = kInfCost;
-    s.goal_best = kInfCost;
-    s.goal_slot = kNone;
-    s.status = ST_RUNNING;
+    team_state_init(&s);
     return s;
 }
 
@@ -104,8 +162,9 @@ int32_t fill_ff(uastar_engine *eng, void *p, size_t bytes) {
 
 struct PlainOut {
     TeamState st;
-    double kernel_ms;
-    uint64_t slots;
+    double kernel_ms;  // all search launches of the solve
+    uint64_t slots;    // final table size
+    int grows;         // in-place table growths
 };
 
 // Run one instance with the whole GPU as the team.  Grows the dedup table /
@@ -123,15 +182,50 @@ template <class P> uint32_t fit_levels(uint32_t H, int levels, size_t budget) {
     return best;
 }
 
+// Heaps of the plain engine when the configuration leaves them to the
+// engine: grids need few (their rounds are bounded by the path length, not
+// by the work per round), puzzles gain throughput from more.
+template <class P> uint32_t plain_heaps(const uastar_config &c) {
+    return c.heaps > 0 ? (uint32_t)c.heaps : (P::kMoves >= 8 ? 8192u : 16384u);
+}
+
+// Moves a paused search's table to one 4x larger (k_grow_*), swapping it in
+// as eng->tab.  Returns false (and changes nothing) if the memory is not there.
+template <class P>
+bool grow_table(uastar_engine *eng, SearchMem<typename P::Entry> &m, uint32_t k, TeamState *st) {
+    const uint64_t old_n = m.mask + 1, new_n = old_n * 4;
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const size_t need = (new_n * sizeof(Slot) > eng->tab_next.bytes ? new_n * sizeof(Slot) : 0) +
+                        (old_n * 4 > eng->grow_map.bytes ? old_n * 4 : 0);
+    if (new_n > (1ull << 32) || need + (256ull << 20) > free_b) return false;
+    if (eng->tab_next.ensure(new_n * sizeof(Slot)) != cudaSuccess) return false;
+    if (eng->grow_map.ensure(old_n * 4) != cudaSuccess) return false;
+    if (fill_ff(eng, eng->tab_next.p, new_n * sizeof(Slot)) != UASTAR_OK) return false;
+    const int blocks = std::max(1, eng->sms * 8);
+    Slot *src = m.tab, *dst = eng->tab_next.as<Slot>();
+    uint32_t *map = eng->grow_map.as<uint32_t>();
+    k_grow_move<<<blocks, 256, 0, eng->stream>>>(src, old_n, dst, new_n - 1, map);
+    k_grow_links<<<blocks, 256, 0, eng->stream>>>(src, old_n, dst, map);
+    k_grow_heaps<P><<<blocks, 256, 0, eng->stream>>>(m.heaps, m.stride, m.L, m.heap_size, k, map, st);
+    eng->launches += 3;
+    if (cudaGetLastError() != cudaSuccess) return false;
+    std::swap(eng->tab, eng->tab_next);
+    m.tab = eng->tab.as<Slot>();
+    m.mask = new_n - 1;
+    m.max_inserted = (uint64_t)((double)new_n * eng->cfg.max_load);
+    return true;
+}
+
 template <class P>
 int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t stride_auto,
                   PlainOut *out) {
     using E = typename P::Entry;
     const uastar_config &c = eng->cfg;
     const uint32_t block = (uint32_t)c.block_threads;
-    const uint32_t tph = c.threads_per_heap > 0 ? (uint32_t)c.threads_per_heap : (P::kMoves >= 8 ? 4u : 2u);
+    const uint32_t tph = c.threads_per_heap > 0 ? (uint32_t)c.threads_per_heap : 4u;
     const uint32_t H = std::max(1u, block / std::min(tph, block));
-    const uint32_t nblocks = (uint32_t)((c.heaps + H - 1) / H);
+    const uint32_t nblocks = (plain_heaps<P>(c) + H - 1) / H;
     const uint32_t k = nblocks * H;
     int log2 = c.hash_log2_slots > 0 ? c.hash_log2_slots : log2_auto;
     uint32_t stride = c.heap_capacity > 0 ? next_pow2_u32((uint32_t)c.heap_capacity + 1) : stride_auto;
@@ -155,12 +249,14 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
         return UASTAR_BAD_INPUT;
     }
     HeapGeometry<P> hg = heap_geometry<P>(L, stride);
+    out->kernel_ms = 0;
+    out->grows = 0;
 
     for (int attempt = 0; attempt < 6; ++attempt) {
         const uint64_t slots = 1ull << log2;
         const size_t tab_b = slots * sizeof(Slot);
         const size_t heap_b = (size_t)k * hg.stride * sizeof(E);
-        const size_t cand_b = (size_t)k * P::kMoves * sizeof(Cand);
+        const size_t cand_b = 2 * (size_t)k * P::kMoves * sizeof(Cand);  // two rounds
         if ((e = eng->tab.ensure(tab_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc table");
         if ((e = eng->heaps.ensure(heap_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc heaps");
         if ((e = eng->heap_size.ensure((size_t)k * 4)) != cudaSuccess) return fail_cuda(eng, e, "alloc heap sizes");
@@ -188,31 +284,47 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
         m.heap_size = eng->heap_size.as<uint32_t>();
         m.cand = eng->cand.as<Cand>();
         m.max_rounds = (uint64_t)c.max_rounds;
+        // an auto-sized table grows in place (x4) when half full
+        const bool auto_table = c.hash_log2_slots <= 0;
+        m.grow_at = auto_table ? slots / 2 : ~0ull;
         TeamState *st = eng->team.as<TeamState>();
         uint64_t timeout_ns = (uint64_t)(c.wait_timeout_s * 1e9);
         P pr = prob;
         uint32_t h_arg = H;
-        void *args[] = {&pr, &m, &st, &timeout_ns, &h_arg};
-        cudaEventRecord(eng->ev0, eng->stream);
-        e = cudaLaunchCooperativeKernel((const void *)k_plain_search<P>, dim3(nblocks), dim3(block),
-                                        args, smem, eng->stream);
-        if (e != cudaSuccess) return fail_cuda(eng, e, "cooperative launch");
-        eng->launches++;
-        cudaEventRecord(eng->ev1, eng->stream);
-        if ((e = cudaMemcpyAsync(&out->st, st, sizeof(TeamState), cudaMemcpyDeviceToHost, eng->stream)) !=
-            cudaSuccess)
-            return fail_cuda(eng, e, "state download");
-        if ((e = cudaStreamSynchronize(eng->stream)) != cudaSuccess) return fail_cuda(eng, e, "search");
-        float ms = 0;
-        cudaEventElapsedTime(&ms, eng->ev0, eng->ev1);
-        out->kernel_ms = ms;
-        out->slots = slots;
+        for (;;) {
+            void *args[] = {&pr, &m, &st, &timeout_ns, &h_arg};
+            cudaEventRecord(eng->ev0, eng->stream);
+            e = cudaLaunchCooperativeKernel((const void *)k_plain_search<P>, dim3(nblocks), dim3(block),
+                                            args, smem, eng->stream);
+            if (e != cudaSuccess) return fail_cuda(eng, e, "cooperative launch");
+            eng->launches++;
+            cudaEventRecord(eng->ev1, eng->stream);
+            if ((e = cudaMemcpyAsync(&out->st, st, sizeof(TeamState), cudaMemcpyDeviceToHost, eng->stream)) !=
+                cudaSuccess)
+                return fail_cuda(eng, e, "state download");
+            if ((e = cudaStreamSynchronize(eng->stream)) != cudaSuccess) return fail_cuda(eng, e, "search");
+            float ms = 0;
+            cudaEventElapsedTime(&ms, eng->ev0, eng->ev1);
+            out->kernel_ms += ms;
+            if (out->st.status != ST_RUNNING) break;
+            // paused for growth
+            if (grow_table<P>(eng, m, k, st)) {
+                out->grows += 1;
+                m.grow_at = (m.mask + 1) / 2;
+            } else {
+                m.grow_at = ~0ull;  // no room: carry on up to the load limit
+                if ((e = cudaMemsetAsync(&st->barrier, 0, sizeof(uint32_t), eng->stream)) != cudaSuccess)
+                    return fail_cuda(eng, e, "state reset");
+            }
+        }
+        out->slots = m.mask + 1;
+        log2 = ceil_log2_u64(out->slots);
 
         const uint32_t s = out->st.status;
         size_t free_b = 0, total_b = 0;
         cudaMemGetInfo(&free_b, &total_b);
-        if (s == ST_HASH_FULL && c.hash_log2_slots <= 0 && log2 < 31 &&
-            (slots * 4 * sizeof(Slot)) < free_b + eng->tab.bytes) {
+        if (s == ST_HASH_FULL && auto_table && log2 < 31 &&
+            (out->slots * 4 * sizeof(Slot)) < free_b + eng->tab.bytes) {
             log2 += 2;
             continue;
         }
@@ -295,8 +407,9 @@ int32_t grid_solve_impl(uastar_engine *eng, const uint64_t *host_words, int32_t 
     prob.ex = ex;
     prob.ey = ey;
     const uint64_t cells = (uint64_t)H * W;
-    const int log2_auto = std::min(28, std::max(16, ceil_log2_u64(cells) - 1));
-    const uint32_t per_heap = (uint32_t)std::min<uint64_t>(8192, std::max<uint64_t>(64, 4 * cells / eng->cfg.heaps));
+    const int log2_auto = std::min(28, std::max(20, ceil_log2_u64(cells) - 1));
+    const uint32_t per_heap =
+        (uint32_t)std::min<uint64_t>(8192, std::max<uint64_t>(64, 4 * cells / plain_heaps<GridProblem>(eng->cfg)));
     PlainOut po;
     int32_t rc = run_plain(eng, prob, log2_auto, next_pow2_u32(per_heap), &po);
     if (rc) return out->status = rc;
@@ -308,6 +421,7 @@ int32_t grid_solve_impl(uastar_engine *eng, const uint64_t *host_words, int32_t 
     out->rounds = (int64_t)st.round;
     out->table_used = (int64_t)st.inserted;
     out->kernel_ms = po.kernel_ms;
+    out->table_grows = po.grows;
     if (st.status == ST_OK) {
         out->straight = (int64_t)(st.goal_best >> 32);
         out->diagonal = (int64_t)(st.goal_best & 0xffffffffu);
@@ -400,7 +514,7 @@ int32_t puzzle_solve_n(uastar_engine *eng, const uint8_t *tiles, uastar_puzzle_r
     prob.pdb = eng->pdb[N].as<uint8_t>();
     prob.start = pack_board(N, tiles);
     prob.goal = PuzzleProblem<N>::goal_key();
-    return run_plain(eng, prob, N == 3 ? 18 : 24, 1024, po);
+    return run_plain(eng, prob, N == 3 ? 20 : 22, N == 3 ? 1024 : 16383, po);
 }
 
 }  // namespace
@@ -417,7 +531,7 @@ uastar_engine *uastar_create(int32_t ordinal, const uastar_config *cfg) {
     eng->device = ordinal;
     if (cfg) eng->cfg = *cfg;
     uastar_config &c = eng->cfg;
-    if (c.heaps <= 0) c.heaps = 8192;
+    if (c.heaps < 0) c.heaps = 0;  // 0: chosen per problem kind (plain_heaps)
     if (c.block_threads <= 0) c.block_threads = 256;
     c.block_threads = std::max(32, std::min(512, (c.block_threads + 31) / 32 * 32));
     if (!(c.max_load > 0.0 && c.max_load < 1.0)) c.max_load = 0.8;
@@ -535,6 +649,7 @@ int32_t uastar_puzzle_solve(uastar_engine *eng, int32_t n, const uint8_t *tiles,
     out->rounds = (int64_t)st.round;
     out->table_used = (int64_t)st.inserted;
     out->kernel_ms = po.kernel_ms;
+    out->table_grows = po.grows;
     if (st.status == ST_OK) {
         out->steps = (int32_t)st.goal_best;
         std::vector<uint64_t> keys;

@@ -56,6 +56,7 @@ struct uastar_engine {
 
     // plain engine buffers
     uastar::DevBuf tab, heaps, heap_size, cand, team, walk, bitmap;
+    uastar::DevBuf tab_next, grow_map;  // table growth of a paused search
     int32_t gH = 0, gW = 0;
     bool grid_loaded = false;
     // pattern databases, indexed by board side

@@ -52,25 +52,49 @@ struct __align__(16) Cand {
 static_assert(sizeof(Cand) == 32, "candidate record");
 
 // Search state shared by the threads of one GA* team (the whole grid for the
-// plain engine, one CTA for the batched engine).  Round-indexed fields are
-// double-buffered by round parity so that they can be reset one round ahead
-// without a third barrier.
+// plain engine, one CTA or cluster for the batched engine).  A round has one
+// team barrier, between its relax phase and its decision; the push phase of
+// round r may still run on one CTA while another is in round r + 1.  So the
+// per-round fields are indexed by round % 3: round r writes its own entry,
+// every CTA reads it after round r's barrier, and CTA 0 clears the entry of
+// round r + 2 during round r's push phase (by then every CTA has read round
+// r - 1's entry, and round r + 2 cannot start before CTA 0 finishes).
 struct __align__(16) TeamState {
-    unsigned long long round_min[2];  // min popped f of the round (cost word)
+    unsigned long long round_min[3];  // min popped f of the round (cost word)
+    unsigned long long goal_min[3];   // min goal f popped in the round
+    unsigned long long ins[3];        // dedup slots claimed in the round
+    uint32_t cand_count[3];           // candidates appended in the round
+    uint32_t err[3];                  // first error of the round's relax phase
+    uint32_t err2[3];                 // first error of the round's push phase (seen by the next decision)
+    uint32_t pad0_;
+    // totals, stored by CTA 0 when the search stops or pauses
     unsigned long long goal_best;     // best goal f popped so far
     unsigned long long round;         // rounds completed
     unsigned long long inserted;      // dedup slots in use
     unsigned long long expanded, generated, pushed;
-    uint32_t cand_count[2];           // candidates appended this round
     uint32_t goal_slot;
-    uint32_t error;                   // first error of phase 1 / barriers (0 = none)
-    uint32_t error2[2];               // first error of phase 2, by round parity
+    uint32_t error;                   // fatal error: barrier timeout, start node not inserted
     uint32_t status;                  // final status (ST_RUNNING while active)
     uint32_t base;                    // heap rotation for pushes
     uint32_t started;                 // start node seeded
     uint32_t barrier;                 // grid-barrier arrival counter
-    uint32_t pad_;
 };
+
+// A fresh team: nothing popped, no goal, no errors.
+__host__ __device__ inline void team_state_init(TeamState *s) {
+    unsigned char *b = reinterpret_cast<unsigned char *>(s);
+    for (unsigned i = 0; i < sizeof(TeamState); ++i) b[i] = 0;
+    for (int i = 0; i < 3; ++i) s->round_min[i] = s->goal_min[i] = kInfCost;
+    s->goal_best = kInfCost;
+    s->goal_slot = kNone;
+    s->status = ST_RUNNING;
+}
+
+// An error recorded by the last round of a paused search that its next
+// decision would report (0 if none).
+__host__ __device__ inline uint32_t team_state_pending_error(uint32_t error, const uint32_t *err2) {
+    return error ? error : (err2[0] ? err2[0] : (err2[1] ? err2[1] : err2[2]));
+}
 
 // ---------------------------------------------------------------- loads ---
 // Cross-SM mutable data is read through L2 (ld.global.cg): L1 is not coherent

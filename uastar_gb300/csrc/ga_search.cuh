@@ -17,14 +17,24 @@
 //            Only a strict improvement makes the successor a candidate, so
 //            among equal-g writers of one slot in a round exactly one
 //            candidate carries the final g.
-//   barrier  then a uniform decision: stop when goal_best <= the round's
-//            minimum popped f (the GA* optimality test of the reference,
-//            src/pathway/GPU-solver.cu:219-243), fail when nothing was popped.
-//   phase 2  CTA c takes candidates c, c + C, c + 2C, ... of the round's n and
-//            deals them round-robin over its own heaps; a candidate is the
-//            slot's winner iff the slot's g still equals its g, and only the
-//            winner writes prev/aux and pushes.
-//   barrier
+//   barrier  then a uniform decision: stop when the best goal f popped so
+//            far <= the round's minimum popped f (the GA* optimality test of
+//            the reference, src/pathway/GPU-solver.cu:219-243), fail when
+//            nothing was popped.
+//   phase 2  CTA c takes candidates c, c + C, c + 2C, ... of the round's n;
+//            its threads check them in parallel (a candidate is the slot's
+//            winner iff the slot's g still equals its g; only the winner
+//            writes prev/aux) and its heap owners push the winners, dealt
+//            round-robin over the CTA's heaps.
+//
+// There is no barrier after phase 2: a CTA that finishes its pushes starts
+// the next round at once.  Its own heaps are all it pops; a relax of round
+// r + 1 that lowers a slot's g while round r's check of that slot is still
+// running only turns round r's candidate into a loser (round r + 1's own
+// candidate for the slot carries the better g), and round r + 1's prev/aux
+// writes come after its barrier, so after every write of round r.  The
+// round-indexed team fields and the candidate buffers are multi-buffered
+// for this (TeamState).
 //
 // Heaps are CTA-private, so the top levels of every heap live in shared
 // memory (a pop touches global memory only below them).
@@ -54,6 +64,11 @@ template <class E> struct SearchMem {
     uint32_t *heap_size;    // k sizes
     Cand *cand;             // >= k * kMoves records
     uint64_t max_rounds;    // absolute round limit (ITER_LIMIT)
+    // A resumable search pauses (returns ST_RUNNING) at the end of the round
+    // in which `inserted` passes grow_at, with the round's candidates pushed
+    // and no work in flight, so that the host can move the table to a larger
+    // one and resume; ~0 = never.
+    uint64_t grow_at = ~0ull;
 };
 
 // ------------------------------------------------------------------ teams ---
@@ -381,13 +396,18 @@ struct PopInfo {
 
 template <class P> struct SearchSmem {
     using E = typename P::Entry;
-    // pops, heap tops, brick scratch, then warp totals
+    // entries of a heap's insertion buffer: two rounds of pushes
+    static constexpr uint32_t kBuf = 2 * P::kMoves;
+    // pops, heap tops, brick scratch, insertion buffers, then warp totals
     static __host__ __device__ size_t tops_offset(uint32_t H) { return (size_t)H * sizeof(PopInfo); }
     static __host__ __device__ size_t scr_offset(uint32_t H, uint32_t L) {
         return (tops_offset(H) + (size_t)H * (1u << L) * sizeof(E) + 127) & ~(size_t)127;
     }
-    static __host__ __device__ size_t scratch_offset(uint32_t H, uint32_t L) {
+    static __host__ __device__ size_t buf_offset(uint32_t H, uint32_t L) {
         return scr_offset(H, L) + (size_t)H * 2 * 128;
+    }
+    static __host__ __device__ size_t scratch_offset(uint32_t H, uint32_t L) {
+        return buf_offset(H, L) + (size_t)H * kBuf * sizeof(E);
     }
     static __host__ __device__ size_t bytes(uint32_t H, uint32_t L) {
         return scratch_offset(H, L) + 4 * (2 + (H + 31) / 32);
@@ -396,8 +416,8 @@ template <class P> struct SearchSmem {
 
 // ------------------------------------------------------------ the search ---
 // Runs up to `budget` rounds (resumable: state lives in TeamState, the heaps
-// and the table).  Returns ST_RUNNING if the budget ran out first, else the
-// final status.  Every thread of every CTA of the team must call it with the
+// and the table).  Returns ST_RUNNING if the budget ran out first or the
+// table passed m.grow_at, else the final status.  Every thread of every CTA of the team must call it with the
 // same H (heaps per CTA, 1 <= H <= blockDim.x); `smem` points at
 // SearchSmem<P>::bytes(H, m.L) bytes of shared memory (128-byte aligned).
 template <class P, class Team>
@@ -425,6 +445,15 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
     E *const gblock = m.heaps + (size_t)(owner ? myh : 0) * m.stride;  // saved top, then bricks
     BrickHeap<P> myheap{gblock + top_reserve<P>(L), tops + (size_t)(owner ? tid : 0) * (1u << L),
                         scr + (size_t)(owner ? tid : 0) * 2 * BrickHeap<P>::BE, L};
+    // The heap's insertion buffer: an unordered list of up to kBuf entries in
+    // shared memory in front of the heap.  The push phase only appends to it;
+    // a pop takes the smaller of the heap's root and the buffer's minimum;
+    // the owner moves entries from the buffer into the heap in the relax
+    // phase (drain), off the round's critical path, keeping room for the next
+    // push phase.  The heap and the buffer together are the priority queue.
+    constexpr uint32_t kBuf = SearchSmem<P>::kBuf;
+    E *const ibuf = reinterpret_cast<E *>(smem + SearchSmem<P>::buf_offset(H, L)) + (size_t)(owner ? tid : 0) * kBuf;
+    uint32_t bn = 0;  // entries in ibuf (owner; empty whenever the search is parked)
     uint64_t nE = 0, nS = 0, nP = 0;
 
     // Every thread reads `started` before the team's rank 0 may set it below,
@@ -458,11 +487,21 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
 
     uint32_t base = team.rd32(&st->base);
     uint64_t round = team.rd64(&st->round);
+    uint64_t gbest = team.rd64(&st->goal_best);     // best goal f over the decided rounds
+    uint64_t ins_total = team.rd64(&st->inserted);  // slots in use after the decided rounds
     uint32_t status = ST_RUNNING;
     uint32_t hs = owner ? ldcg_u32(&m.heap_size[myh]) : 0;  // this owner's heap size (private)
+    // candidates: two buffers of C * H * kMoves records, by round parity (a
+    // CTA may append round r + 1's while another still reads round r's)
+    const uint32_t cand_half = C * H * P::kMoves;
+    // push-phase staging: one entry per candidate of this CTA's share (at most
+    // H * kMoves); it reuses the sift-down scratch, idle in that phase
+    static_assert(2 * BrickHeap<P>::BE >= P::kMoves, "staging fits the sift scratch");
+    E *const stage = scr;
 
     for (uint64_t it = 0;; ++it) {
-        const uint32_t par = (uint32_t)(round & 1);
+        const uint32_t r3 = (uint32_t)(round % 3);
+        Cand *const cand = m.cand + (size_t)(round & 1) * cand_half;
 
         // ------------------------------------------------ phase 1: pop ---
         // The owner takes the root now and refills the hole later in the
@@ -472,16 +511,25 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         if (tid < owner_warps * 32u) {
             E e;
             uint32_t mv = 0;
-            const bool have = owner && hs > 0;
+            const bool have = owner && (hs > 0 || bn > 0);
             if (have) {
-                e = myheap.s[1];
-                last = myheap.ld(hs);
-                hs -= 1;
-                pending_sift = hs > 0;
+                uint32_t bi = 0;
+                for (uint32_t j = 1; j < bn; ++j)
+                    if (P::less(ibuf[j], ibuf[bi])) bi = j;
+                if (hs > 0 && (bn == 0 || !P::less(ibuf[bi], myheap.s[1]))) {
+                    e = myheap.s[1];
+                    last = myheap.ld(hs);
+                    hs -= 1;
+                    pending_sift = hs > 0;
+                } else {
+                    e = ibuf[bi];
+                    ibuf[bi] = ibuf[bn - 1];
+                    bn -= 1;
+                }
             }
             const uint64_t ecost = have ? P::entry_cost(e) : kInfCost;
             const uint64_t wmin = warp_min_cost<P>(ecost);
-            if (lane == 0 && wmin != kInfCost) atomic_min_cost<P>(&st->round_min[par], wmin);
+            if (lane == 0 && wmin != kInfCost) atomic_min_cost<P>(&st->round_min[r3], wmin);
             if (have) {
                 uint64_t key, g;
                 uint32_t aux;
@@ -490,7 +538,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                 if (fcur != ecost) {
                     // stale: the node was improved after this entry was pushed
                 } else if (prob.is_goal(key)) {
-                    atomic_min_cost<P>(&st->goal_best, fcur);
+                    atomic_min_cost<P>(&st->goal_min[r3], fcur);
                     st->goal_slot = e.slot;  // every goal pop names the same slot
                 } else {
                     ++nE;
@@ -532,7 +580,20 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         __syncthreads();
 
         // ------------------ phase 1: relax successors / refill heap roots ---
-        if (rfirst > 0 && pending_sift) heap_sift_down<P>(myheap, hs, last);
+        // Owner chores of the round, while the other warps relax: refill the
+        // root hole, then drain the insertion buffer down to kBuf - kMoves
+        // entries (room for this round's pushes).
+        const auto chores = [&]() {
+            if (pending_sift) heap_sift_down<P>(myheap, hs, last);
+            while (bn > kBuf - P::kMoves) {
+                if (hs + 1 > m.hcap) {
+                    set_error(&st->err[r3], ST_HEAP_OVERFLOW);  // this round's decision stops the search
+                    break;
+                }
+                heap_push<P>(myheap, hs, ibuf[--bn]);
+            }
+        };
+        if (rfirst > 0 && owner) chores();
         if (relaxer) {
             const uint32_t rt = tid - rfirst;
             for (uint32_t b0 = 0; b0 < total; b0 += rthreads) {
@@ -558,7 +619,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                     ++nS;
                     const int r = relax<P>(m.tab, m.mask, m.max_probe, nkey, ng, &nslot);
                     if (r == RELAX_FULL) {
-                        set_error(&st->error, ST_HASH_FULL);
+                        set_error(&st->err[r3], ST_HASH_FULL);
                     } else {
                         inserted = (r == RELAX_INSERTED);
                         improved = (r & RELAX_IMPROVED) != 0;
@@ -566,14 +627,14 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                 }
                 const uint32_t ib = __ballot_sync(kFull, inserted);
                 if (ib && lane == (uint32_t)(__ffs(ib) - 1)) {
-                    const unsigned long long before = atomicAdd(&st->inserted, (unsigned long long)__popc(ib));
-                    if (before + __popc(ib) > m.max_inserted) set_error(&st->error, ST_HASH_FULL);
+                    const unsigned long long before = atomicAdd(&st->ins[r3], (unsigned long long)__popc(ib));
+                    if (ins_total + before + __popc(ib) > m.max_inserted) set_error(&st->err[r3], ST_HASH_FULL);
                 }
                 const uint32_t bal = __ballot_sync(kFull, improved);
                 if (bal) {
                     const uint32_t leader = (uint32_t)(__ffs(bal) - 1);
                     uint32_t cbase = 0;
-                    if (lane == leader) cbase = atomicAdd(&st->cand_count[par], (uint32_t)__popc(bal));
+                    if (lane == leader) cbase = atomicAdd(&st->cand_count[r3], (uint32_t)__popc(bal));
                     cbase = __shfl_sync(kFull, cbase, leader);
                     if (improved) {
                         Cand c;
@@ -583,25 +644,28 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                         c.f = nf;
                         c.aux = naux;
                         c.pad = 0;
-                        m.cand[cbase + __popc(bal & lanemask_lt())] = c;
+                        cand[cbase + __popc(bal & lanemask_lt())] = c;
                     }
                 }
             }
         }
-        if (rfirst == 0 && pending_sift) heap_sift_down<P>(myheap, hs, last);
+        if (rfirst == 0 && owner) chores();
 
         team.sync();
 
         // -------------------------------------------------- decision ---
-        // Every value read here is written only before the barrier above or
-        // after the next one, so all threads decide alike.  Phase-2 errors of
-        // round r are written to error2[r & 1] and read at the decision of
-        // round r + 1.
-        const uint64_t rmin = team.rd64(&st->round_min[par]);
-        const uint64_t gbest = team.rd64(&st->goal_best);
-        uint32_t err = team.rd32(&st->error);
-        if (!err) err = team.rd32(&st->error2[par ^ 1]);
-        const uint32_t ncand = team.rd32(&st->cand_count[par]);
+        // Every value read here was written before the barrier above and is
+        // not written again before every CTA has read it (see TeamState), so
+        // all threads decide alike.
+        const uint64_t rmin = team.rd64(&st->round_min[r3]);
+        const uint64_t gmin = team.rd64(&st->goal_min[r3]);
+        if (P::cost_cmp(gmin, gbest) < 0) gbest = gmin;
+        uint32_t err = team.rd32(&st->err[r3]);
+        if (!err) err = team.rd32(&st->err2[(r3 + 2) % 3]);  // the previous round's push phase
+        if (!err) err = team.rd32(&st->error);
+        const uint32_t ncand = team.rd32(&st->cand_count[r3]);
+        ins_total += team.rd64(&st->ins[r3]);
+        const bool pause = ins_total > m.grow_at;
         round += 1;
         if (err) {
             status = err;
@@ -622,33 +686,59 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
 
         // ---------------------------------------------------- phase 2 ---
         if (cta == 0 && tid == 0) {
-            st->round_min[par ^ 1] = kInfCost;
-            st->cand_count[par ^ 1] = 0;
+            const uint32_t a = (r3 + 2) % 3;  // the round after next
+            st->round_min[a] = kInfCost;
+            st->goal_min[a] = kInfCost;
+            st->ins[a] = 0;
+            st->cand_count[a] = 0;
+            st->err[a] = 0;
+            st->err2[(r3 + 1) % 3] = 0;  // last read by this round's predecessor's decision
         }
-        if (owner) {
-            // This CTA's share of the round's candidates is every C-th one
-            // (a contiguous chunk would hold the successors of a few warps'
-            // pops, i.e. one small region of the search, and starve the rest
-            // of the team's heaps of it); the share is dealt over its heaps.
-            for (uint32_t i = cta + C * ((tid + base) % H); i < ncand; i += C * H) {
-                const Cand c = load_cand(m.cand + i);
-                if (ldcg_u64(&m.tab[c.slot].g) != c.g) continue;  // lost to a better writer
+        // This CTA's share of the round's candidates is every C-th one (a
+        // contiguous chunk would hold the successors of a few warps' pops,
+        // i.e. one small region of the search, and starve the rest of the
+        // team's heaps of it).  All threads check a part of the share: a
+        // candidate is the slot's winner iff the slot's g still equals its g;
+        // winners write prev/aux and are staged for their heap's owner.
+        const uint32_t nshare = ncand > cta ? (ncand - cta + C - 1) / C : 0u;
+        for (uint32_t q = tid; q < nshare; q += T) {
+            const Cand c = load_cand(cand + cta + (size_t)C * q);
+            E e = prob.make_entry(c.f, c.g, c.slot);
+            if (ldcg_u64(&m.tab[c.slot].g) == c.g) {
                 m.tab[c.slot].prev = c.parent;
                 m.tab[c.slot].aux = c.aux;
-                if (hs + 1 > m.hcap) {
-                    set_error(&st->error2[par], ST_HEAP_OVERFLOW);
-                    break;
-                }
-                heap_push<P>(myheap, hs, prob.make_entry(c.f, c.g, c.slot));
+            } else {
+                e.slot = kNone;  // lost to a better writer
+            }
+            stage[q] = e;
+        }
+        __syncthreads();
+        // The share is dealt round-robin over the CTA's heaps (at most
+        // kMoves per heap: the share is at most H * kMoves) into their
+        // insertion buffers, which the relax phase left with room for kMoves.
+        if (owner) {
+            for (uint32_t q = (tid + base) % H; q < nshare; q += H) {
+                const E e = stage[q];
+                if (e.slot == kNone) continue;
+                ibuf[bn++] = e;
                 ++nP;
             }
         }
         base = (uint32_t)(((uint64_t)base + ncand) % H);
-        team.sync();
-        if (it + 1 >= budget) break;
+        if (pause || it + 1 >= budget) break;
     }
 
-    // Persist the resumable state: sizes and the shared tops.
+    // Persist the resumable state: the buffers go into the heaps, then the
+    // sizes and the shared tops.
+    if (owner && status == ST_RUNNING) {
+        while (bn > 0) {
+            if (hs + 1 > m.hcap) {
+                set_error(&st->error, ST_HEAP_OVERFLOW);  // reported by the next decision
+                break;
+            }
+            heap_push<P>(myheap, hs, ibuf[--bn]);
+        }
+    }
     if (owner) {
         m.heap_size[myh] = hs;
         for (uint32_t i = 1; i <= topn && i <= hs; ++i) P::store(gblock + i, myheap.s[i]);
@@ -656,6 +746,8 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
     if (cta == 0 && tid == 0) {
         st->round = round;
         st->base = base;
+        st->goal_best = gbest;
+        st->inserted = ins_total;
         if (status != ST_RUNNING) st->status = status;
     }
     // Flush statistics: one atomic per warp.

@@ -52,7 +52,7 @@ constexpr uint32_t kHeapStride = 4672;
 constexpr size_t kOffState = 0;
 constexpr size_t kOffSizes = align256(kOffState + sizeof(TeamState));
 constexpr size_t kOffCand = align256(kOffSizes + kHeaps * sizeof(uint32_t));
-constexpr size_t kOffHeaps = align256(kOffCand + (size_t)kHeaps * GridProblem::kMoves * sizeof(Cand));
+constexpr size_t kOffHeaps = align256(kOffCand + 2 * (size_t)kHeaps * GridProblem::kMoves * sizeof(Cand));
 constexpr size_t kOffTable = align256(kOffHeaps + (size_t)kHeaps * kHeapStride * sizeof(GridEntry));
 constexpr size_t kScratchBytes = align256(kOffTable + kTableSlots * sizeof(Slot));
 
@@ -69,13 +69,7 @@ __global__ void k_noalloc_reset(unsigned char *scratch) {
     TeamState *st = reinterpret_cast<TeamState *>(scratch + kOffState);
     uint32_t *sizes = reinterpret_cast<uint32_t *>(scratch + kOffSizes);
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t == 0) {
-        memset(st, 0, sizeof(TeamState));
-        st->round_min[0] = st->round_min[1] = kInfCost;
-        st->goal_best = kInfCost;
-        st->goal_slot = kNone;
-        st->status = ST_RUNNING;
-    }
+    if (t == 0) team_state_init(st);
     for (uint32_t i = t; i < kHeaps; i += gridDim.x * blockDim.x) sizes[i] = 0;
     // dedup table: every slot empty (key and g all ones, prev = none)
     uint4 *tab = reinterpret_cast<uint4 *>(scratch + kOffTable);

@@ -131,6 +131,7 @@ class GridSolution:
     path_len: int
     kernel_ms: float
     solve_ms: float
+    table_grows: int = 0
 
     @property
     def ok(self) -> bool:
@@ -148,6 +149,7 @@ class PuzzleSolution:
     table_used: int
     kernel_ms: float
     solve_ms: float
+    table_grows: int = 0
 
     @property
     def ok(self) -> bool:
@@ -248,7 +250,8 @@ class Engine:
 
     def _grid_sol(self, r: L.GridResult) -> GridSolution:
         return GridSolution(r.status, r.straight, r.diagonal, r.cost, r.cost_exact, r.expanded, r.generated,
-                            r.pushed, r.rounds, r.table_used, r.path_len, r.kernel_ms, r.solve_ms)
+                            r.pushed, r.rounds, r.table_used, r.path_len, r.kernel_ms, r.solve_ms,
+                            r.table_grows)
 
     def grid_solve_loaded(self, start, goal) -> GridSolution:
         r = L.GridResult()
@@ -299,7 +302,7 @@ class Engine:
         if r.status in (L.CUDA_ERROR, L.BAD_INPUT, L.TIMEOUT):
             raise EngineError(r.status, self.last_error)
         return PuzzleSolution(r.status, r.steps, r.expanded, r.generated, r.pushed, r.rounds, r.table_used,
-                              r.kernel_ms, r.solve_ms)
+                              r.kernel_ms, r.solve_ms, r.table_grows)
 
     def puzzle_moves(self) -> list[int]:
         n = self._lib.uastar_puzzle_moves(self._h, None, 0)
