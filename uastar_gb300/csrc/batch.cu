@@ -70,7 +70,7 @@ struct BatchArgs {
     uint8_t *heaps;        // per CTA: H heaps x slice bytes
     uint64_t slice;        // bytes per heap (batch)
     uint32_t *hsize;       // per CTA: H
-    Cand *cand;            // per CTA: 2 * H * 8 (two rounds)
+    Cand *cand;            // per CTA: 2 * (8 H + 1) records (cand_records with 8 moves)
     uint32_t H;            // heaps per instance (CTA)
     uint32_t L_grid, L_puzzle;            // heap levels in shared memory
     uint32_t stride_grid, stride_puzzle;  // batch heap geometry per entry type
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
     // serving: each request owns a slice named by its descriptor
     uint8_t *heaps = a.heaps + (size_t)blockIdx.x * H * a.slice;
     uint32_t *hs = a.hsize + (size_t)blockIdx.x * H;
-    Cand *cand = a.cand + (size_t)blockIdx.x * H * 16;
+    Cand *cand = a.cand + (size_t)blockIdx.x * 2 * (8 * H + 1);
     for (uint32_t iter = 0;; ++iter) {
         if (a.serving) {
             if (iter > 0 || blockIdx.x >= a.count) break;
@@ -199,8 +199,8 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
             o.t_start = t_start;
             o.t_end = globaltimer_ns();
             // a phase-2 error of the last round of a quantum is still in error2
-            const uint32_t pend = team_state_pending_error(st.error, st.err2);
-            if (o.status == ST_RUNNING && pend) o.status = pend;
+            // an error of a parked search is reported by its next decision: report it now
+            if (o.status == ST_RUNNING && st.error) o.status = st.error;
             // batch: the region is reused by the next instance, so the path
             // is read out now
             if (!a.serving && o.status == ST_OK) o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap);
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(512, 1) k_batch_cluster(BatchArgs a) {
     ClusterTeam team{st};
     uint8_t *heaps = a.heaps + (size_t)cid * csize * H * a.slice;
     uint32_t *hs = a.hsize + (size_t)cid * csize * H;
-    Cand *cand = a.cand + (size_t)cid * csize * H * 16;
+    Cand *cand = a.cand + (size_t)cid * csize * 2 * (8 * H + 1);
     for (uint32_t iter = 0;; ++iter) {
         uint32_t i;
         if (a.serving) {
@@ -270,8 +270,7 @@ __global__ void __launch_bounds__(512, 1) k_batch_cluster(BatchArgs a) {
             o.inserted = ldcg_u64(&st->inserted);
             o.t_start = t_start;
             o.t_end = globaltimer_ns();
-            const uint32_t e2[3] = {ldcg_u32(&st->err2[0]), ldcg_u32(&st->err2[1]), ldcg_u32(&st->err2[2])};
-            const uint32_t pend = team_state_pending_error(ldcg_u32(&st->error), e2);
+            const uint32_t pend = ldcg_u32(&st->error);
             if (o.status == ST_RUNNING && pend) o.status = pend;
             if (!a.serving && o.status == ST_OK) o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap);
             a.outs[i] = o;
@@ -535,7 +534,7 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
     if ((e = eng->b_tab.ensure(tab_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc partitions");
     if ((e = eng->b_heaps.ensure(heap_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc heap slices");
     if ((e = eng->b_hsize.ensure((size_t)g.ctas * g.H * 4)) != cudaSuccess) return fail_cuda(eng, e, "alloc");
-    if ((e = eng->b_cand.ensure((size_t)g.ctas * g.H * 16 * sizeof(Cand))) != cudaSuccess)
+    if ((e = eng->b_cand.ensure((size_t)g.ctas * 2 * (8 * g.H + 1) * sizeof(Cand))) != cudaSuccess)
         return fail_cuda(eng, e, "alloc");
     if ((e = eng->b_desc.ensure(cnt * sizeof(InstDesc))) != cudaSuccess) return fail_cuda(eng, e, "alloc");
     if ((e = eng->b_out.ensure(cnt * sizeof(InstOut))) != cudaSuccess) return fail_cuda(eng, e, "alloc");
@@ -1527,7 +1526,7 @@ int32_t uastar_serve_start(uastar_engine *eng, const uastar_serve_config *cfg) {
             (e = t.d_outs.ensure((size_t)t.nslots * sizeof(InstOut))) != cudaSuccess ||
             (e = t.d_states.ensure((size_t)t.nslots * sizeof(TeamState))) != cudaSuccess ||
             (e = t.d_hsize.ensure(ctas * t.geo.H * 4)) != cudaSuccess ||
-            (e = t.d_cand.ensure(ctas * t.geo.H * 16 * sizeof(Cand))) != cudaSuccess ||
+            (e = t.d_cand.ensure(ctas * 2 * (8 * t.geo.H + 1) * sizeof(Cand))) != cudaSuccess ||
             (e = cudaStreamCreateWithFlags(&t.stream, cudaStreamNonBlocking)) != cudaSuccess ||
             (e = cudaEventCreate(&t.e0)) != cudaSuccess || (e = cudaEventCreate(&t.e1)) != cudaSuccess)
             break;

@@ -244,6 +244,10 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
     int max_active = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_active, k_plain_search<P>, (int)block, smem);
     if (e != cudaSuccess) return fail_cuda(eng, e, "occupancy");
+    if (nblocks + 1 > 32 * H) {  // the push phase keeps nblocks + 1 region offsets in shared memory
+        eng->set_err("too many CTAs for the heaps per CTA (need CTAs < 32 * block_threads / threads_per_heap)");
+        return UASTAR_BAD_INPUT;
+    }
     if ((uint64_t)max_active * eng->sms < nblocks) {
         eng->set_err("heaps / (block_threads / threads_per_heap) exceed one co-resident wave of the GPU");
         return UASTAR_BAD_INPUT;
@@ -256,7 +260,7 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
         const uint64_t slots = 1ull << log2;
         const size_t tab_b = slots * sizeof(Slot);
         const size_t heap_b = (size_t)k * hg.stride * sizeof(E);
-        const size_t cand_b = 2 * (size_t)k * P::kMoves * sizeof(Cand);  // two rounds
+        const size_t cand_b = cand_records<P>(nblocks, H) * sizeof(Cand);
         if ((e = eng->tab.ensure(tab_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc table");
         if ((e = eng->heaps.ensure(heap_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc heaps");
         if ((e = eng->heap_size.ensure((size_t)k * 4)) != cudaSuccess) return fail_cuda(eng, e, "alloc heap sizes");

@@ -63,9 +63,7 @@ struct __align__(16) TeamState {
     unsigned long long round_min[3];  // min popped f of the round (cost word)
     unsigned long long goal_min[3];   // min goal f popped in the round
     unsigned long long ins[3];        // dedup slots claimed in the round
-    uint32_t cand_count[3];           // candidates appended in the round
     uint32_t err[3];                  // first error of the round's relax phase
-    uint32_t err2[3];                 // first error of the round's push phase (seen by the next decision)
     uint32_t pad0_;
     // totals, stored by CTA 0 when the search stops or pauses
     unsigned long long goal_best;     // best goal f popped so far
@@ -73,7 +71,8 @@ struct __align__(16) TeamState {
     unsigned long long inserted;      // dedup slots in use
     unsigned long long expanded, generated, pushed;
     uint32_t goal_slot;
-    uint32_t error;                   // fatal error: barrier timeout, start node not inserted
+    uint32_t error;                   // fatal error: barrier timeout, start node not inserted,
+                                      // heap overflow while parking the insertion buffers
     uint32_t status;                  // final status (ST_RUNNING while active)
     uint32_t base;                    // heap rotation for pushes
     uint32_t started;                 // start node seeded
@@ -88,12 +87,6 @@ __host__ __device__ inline void team_state_init(TeamState *s) {
     s->goal_best = kInfCost;
     s->goal_slot = kNone;
     s->status = ST_RUNNING;
-}
-
-// An error recorded by the last round of a paused search that its next
-// decision would report (0 if none).
-__host__ __device__ inline uint32_t team_state_pending_error(uint32_t error, const uint32_t *err2) {
-    return error ? error : (err2[0] ? err2[0] : (err2[1] ? err2[1] : err2[2]));
 }
 
 // ---------------------------------------------------------------- loads ---

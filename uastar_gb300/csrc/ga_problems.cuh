@@ -105,6 +105,20 @@ struct GridProblem {
         naux = 0;
         nf = ng + h_of(nkey);
     }
+    // Successor in two steps (the puzzle's second step waits on a database
+    // load that is issued in the first, so that it overlaps the table CAS);
+    // for grids everything is register arithmetic in the first.
+    struct Succ {
+        uint64_t key, g, f;
+    };
+    __device__ __forceinline__ void succ_begin(uint64_t key, uint64_t g, uint32_t aux, int mv, Succ &s) const {
+        uint32_t naux;
+        apply(key, g, aux, mv, s.key, s.g, naux, s.f);
+    }
+    __device__ __forceinline__ void succ_end(const Succ &s, uint32_t, int, uint32_t &naux, uint64_t &nf) const {
+        naux = 0;
+        nf = s.f;
+    }
     __device__ __forceinline__ Entry make_entry(uint64_t f, uint64_t g, uint32_t slot) const {
         Entry e;
         e.fa = (uint32_t)(f >> 32);
@@ -274,6 +288,33 @@ template <int N> struct PuzzleProblem {
         naux = a | ((uint32_t)(mv + 1) << 16);
         ng = g + 1;
         nf = ng + hsum(naux);
+    }
+    // Two-step successor (see GridProblem::Succ): the first step computes the
+    // board and issues the load of the moved tile's pattern entry, the second
+    // (after the table CAS) folds it into aux and f.
+    struct Succ {
+        uint64_t key, g;
+        uint32_t part;  // the loaded pattern entry
+        uint32_t which; // its pattern
+    };
+    __device__ __forceinline__ void succ_begin(uint64_t key, uint64_t g, uint32_t, int mv, Succ &s) const {
+        const int b = blank(key);
+        const int q = b + (mv == 0 ? N : mv == 1 ? -N : mv == 2 ? 1 : -1);
+        const uint64_t t = (key >> (4 * q)) & 15;
+        s.key = (key & ~(15ull << (4 * q))) | (t << (4 * b));
+        s.g = g + 1;
+        s.which = (uint32_t)pattern_of_tile<N>((int)t);
+        s.part = part((int)s.which, inverse(s.key));
+    }
+    __device__ __forceinline__ void succ_end(const Succ &s, uint32_t aux, int mv, uint32_t &naux,
+                                             uint64_t &nf) const {
+        uint32_t a = aux & 0xffffu;
+        if (s.which == 0)
+            a = (a & 0xff00u) | s.part;
+        else
+            a = (a & 0x00ffu) | (s.part << 8);
+        naux = a | ((uint32_t)(mv + 1) << 16);
+        nf = s.g + hsum(naux);
     }
     __device__ __forceinline__ Entry make_entry(uint64_t f, uint64_t g, uint32_t slot) const {
         Entry e;

@@ -62,7 +62,7 @@ template <class E> struct SearchMem {
     uint32_t hcap;          // maximum heap size
     uint32_t L;             // heap levels kept in shared memory (>= 1)
     uint32_t *heap_size;    // k sizes
-    Cand *cand;             // >= k * kMoves records
+    Cand *cand;             // cand_records<P>(C, H) records
     uint64_t max_rounds;    // absolute round limit (ITER_LIMIT)
     // A resumable search pauses (returns ST_RUNNING) at the end of the round
     // in which `inserted` passes grow_at, with the round's candidates pushed
@@ -241,18 +241,58 @@ __device__ __forceinline__ void heap_sift_down(const BrickHeap<P> &h, uint32_t s
     h.st(now, last);
 }
 
+// Insert v.  Below the shared top the climb works brick by brick: the brick
+// holding the current position is read once (one burst of independent loads)
+// into scratch half 0, the climb inside it runs in shared memory and the
+// brick is written back, so a push waits on global memory once per brick it
+// climbs through (most climb none or one) instead of once per level.
 template <class P>
 __device__ __forceinline__ void heap_push(const BrickHeap<P> &h, uint32_t &size, const typename P::Entry &v) {
     using E = typename P::Entry;
+    constexpr uint32_t D = BrickHeap<P>::D;
     uint32_t now = ++size;
+    const uint32_t topn = h.topn();
+    while (now > topn) {
+        const uint32_t l = 31u - (uint32_t)__clz(now);
+        const uint32_t r = l - h.L;
+        const uint32_t d = r - (r / D) * D;  // depth of `now` in its brick
+        const uint32_t root = now >> d;
+        h.fetch(root, 0);
+        E *const b = h.scr;
+        uint4 *const gl = reinterpret_cast<uint4 *>(h.g + h.off(root) - 1);
+        uint32_t loc = (1u << d) | (now & ((1u << d) - 1u));
+        while (loc > 1) {
+            const E pv = b[loc >> 1];
+            if (!P::less(v, pv)) break;
+            b[loc] = pv;
+            loc >>= 1;
+            now >>= 1;
+        }
+        bool done = loc > 1;
+        if (!done) {
+            // at the brick's root: its parent is in the brick above or the shared top
+            const E pv = h.ld(now >> 1);
+            if (!P::less(v, pv)) {
+                done = true;
+            } else {
+                b[1] = pv;
+                now >>= 1;
+            }
+        }
+        if (done) b[loc] = v;
+        const uint4 *src = reinterpret_cast<const uint4 *>(b);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) gl[q] = src[q];
+        if (done) return;
+    }
     while (now > 1) {
         const uint32_t par = now >> 1;
-        const E pv = h.ld(par);
+        const E pv = h.s[par];
         if (!P::less(v, pv)) break;
-        h.st(now, pv);
+        h.s[now] = pv;
         now = par;
     }
-    h.st(now, v);
+    h.s[now] = v;
 }
 
 // Global entries per heap and the largest heap size for L shared levels and
@@ -394,6 +434,16 @@ struct PopInfo {
     uint32_t aux, slot, mask, excl;  // excl: exclusive prefix of successor counts
 };
 
+// Candidate records of a team of C CTAs with H heaps each: two buffers (by
+// round parity) of C regions, one per CTA, each a header record (its count
+// in .slot) and room for the successors of the CTA's H pops.
+template <class P> __host__ __device__ constexpr uint64_t cand_region_records(uint32_t H) {
+    return (uint64_t)H * P::kMoves + 1;
+}
+template <class P> __host__ __device__ constexpr uint64_t cand_records(uint32_t C, uint32_t H) {
+    return 2ull * C * cand_region_records<P>(H);
+}
+
 template <class P> struct SearchSmem {
     using E = typename P::Entry;
     // entries of a heap's insertion buffer: two rounds of pushes
@@ -409,10 +459,41 @@ template <class P> struct SearchSmem {
     static __host__ __device__ size_t scratch_offset(uint32_t H, uint32_t L) {
         return buf_offset(H, L) + (size_t)H * kBuf * sizeof(E);
     }
+    // warp totals of the block scans, then this CTA's round counters
+    static constexpr uint32_t kScratchWords = 40;
     static __host__ __device__ size_t bytes(uint32_t H, uint32_t L) {
-        return scratch_offset(H, L) + 4 * (2 + (H + 31) / 32);
+        return scratch_offset(H, L) + 4 * kScratchWords;
     }
 };
+
+// Exclusive prefix sum over the CTA of one value per thread (blockDim.x a
+// multiple of 32, at most 1024); *total gets the sum.  Uses scratch[0] and
+// scratch[2 .. 2 + warps).
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *scratch, uint32_t *total) {
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= (uint32_t)o) incl += t;
+    }
+    if (lane == 31) scratch[2 + w] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (uint32_t q = 0; q < nw; ++q) {
+            const uint32_t t = scratch[2 + q];
+            scratch[2 + q] = acc;
+            acc += t;
+        }
+        scratch[0] = acc;
+    }
+    __syncthreads();
+    const uint32_t off = scratch[2 + w] + incl - v;
+    *total = scratch[0];
+    __syncthreads();
+    return off;
+}
 
 // ------------------------------------------------------------ the search ---
 // Runs up to `budget` rounds (resumable: state lives in TeamState, the heaps
@@ -491,17 +572,28 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
     uint64_t ins_total = team.rd64(&st->inserted);  // slots in use after the decided rounds
     uint32_t status = ST_RUNNING;
     uint32_t hs = owner ? ldcg_u32(&m.heap_size[myh]) : 0;  // this owner's heap size (private)
-    // candidates: two buffers of C * H * kMoves records, by round parity (a
-    // CTA may append round r + 1's while another still reads round r's)
-    const uint32_t cand_half = C * H * P::kMoves;
-    // push-phase staging: one entry per candidate of this CTA's share (at most
-    // H * kMoves); it reuses the sift-down scratch, idle in that phase
+    // Candidates: two buffers by round parity (a CTA may append round r + 1's
+    // while another still reads round r's), each one region per CTA (its
+    // header record holds the count), so a relaxing warp claims room with a
+    // shared-memory atomic and the CTA publishes one count per round.
+    const uint64_t RR = cand_region_records<P>(H);
+    uint32_t *const s_cnt = scratch + 36;  // this CTA's candidates this round
+    uint32_t *const s_ins = scratch + 37;  // dedup slots it claimed this round
+    // Push-phase staging: one entry per candidate of this CTA's share (at most
+    // H * kMoves), then the C + 1 region offsets of the round's candidates
+    // (the host keeps C < 32 H); it reuses the sift-down scratch, idle then.
     static_assert(2 * BrickHeap<P>::BE >= P::kMoves, "staging fits the sift scratch");
     E *const stage = scr;
+    uint32_t *const roff = reinterpret_cast<uint32_t *>(scr + (size_t)H * P::kMoves);
 
     for (uint64_t it = 0;; ++it) {
         const uint32_t r3 = (uint32_t)(round % 3);
-        Cand *const cand = m.cand + (size_t)(round & 1) * cand_half;
+        Cand *const half = m.cand + (size_t)(round & 1) * C * RR;
+        Cand *const myreg = half + (size_t)cta * RR + 1;
+        if (tid == 0) {
+            *s_cnt = 0;
+            *s_ins = 0;
+        }
 
         // ------------------------------------------------ phase 1: pop ---
         // The owner takes the root now and refills the hole later in the
@@ -590,7 +682,13 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                     set_error(&st->err[r3], ST_HEAP_OVERFLOW);  // this round's decision stops the search
                     break;
                 }
-                heap_push<P>(myheap, hs, ibuf[--bn]);
+                // move the buffer's largest entry (the small ones are popped soon)
+                uint32_t bx = 0;
+                for (uint32_t j = 1; j < bn; ++j)
+                    if (P::less(ibuf[bx], ibuf[j])) bx = j;
+                const E e = ibuf[bx];
+                ibuf[bx] = ibuf[--bn];
+                heap_push<P>(myheap, hs, e);
             }
         };
         if (rfirst > 0 && owner) chores();
@@ -614,10 +712,12 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                     const PopInfo &pi = pop[lo];
                     const int move = (int)__fns(pi.mask, 0, (int)(j - pi.excl) + 1);
                     oslot = pi.slot;
-                    uint64_t nkey;
-                    prob.apply(pi.key, pi.g, pi.aux, move, nkey, ng, naux, nf);
+                    typename P::Succ sc;
+                    prob.succ_begin(pi.key, pi.g, pi.aux, move, sc);
+                    ng = sc.g;
                     ++nS;
-                    const int r = relax<P>(m.tab, m.mask, m.max_probe, nkey, ng, &nslot);
+                    const int r = relax<P>(m.tab, m.mask, m.max_probe, sc.key, sc.g, &nslot);
+                    prob.succ_end(sc, pi.aux, move, naux, nf);
                     if (r == RELAX_FULL) {
                         set_error(&st->err[r3], ST_HASH_FULL);
                     } else {
@@ -626,15 +726,12 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                     }
                 }
                 const uint32_t ib = __ballot_sync(kFull, inserted);
-                if (ib && lane == (uint32_t)(__ffs(ib) - 1)) {
-                    const unsigned long long before = atomicAdd(&st->ins[r3], (unsigned long long)__popc(ib));
-                    if (ins_total + before + __popc(ib) > m.max_inserted) set_error(&st->err[r3], ST_HASH_FULL);
-                }
+                if (ib && lane == (uint32_t)(__ffs(ib) - 1)) atomicAdd(s_ins, (uint32_t)__popc(ib));
                 const uint32_t bal = __ballot_sync(kFull, improved);
                 if (bal) {
                     const uint32_t leader = (uint32_t)(__ffs(bal) - 1);
                     uint32_t cbase = 0;
-                    if (lane == leader) cbase = atomicAdd(&st->cand_count[r3], (uint32_t)__popc(bal));
+                    if (lane == leader) cbase = atomicAdd(s_cnt, (uint32_t)__popc(bal));
                     cbase = __shfl_sync(kFull, cbase, leader);
                     if (improved) {
                         Cand c;
@@ -644,13 +741,19 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                         c.f = nf;
                         c.aux = naux;
                         c.pad = 0;
-                        cand[cbase + __popc(bal & lanemask_lt())] = c;
+                        myreg[cbase + __popc(bal & lanemask_lt())] = c;
                     }
                 }
             }
         }
         if (rfirst == 0 && owner) chores();
 
+        // publish this CTA's round: its candidate count and claimed slots
+        __syncthreads();
+        if (tid == 0) {
+            half[(size_t)cta * RR].slot = *s_cnt;
+            if (*s_ins) atomicAdd(&st->ins[r3], (unsigned long long)*s_ins);
+        }
         team.sync();
 
         // -------------------------------------------------- decision ---
@@ -661,10 +764,9 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         const uint64_t gmin = team.rd64(&st->goal_min[r3]);
         if (P::cost_cmp(gmin, gbest) < 0) gbest = gmin;
         uint32_t err = team.rd32(&st->err[r3]);
-        if (!err) err = team.rd32(&st->err2[(r3 + 2) % 3]);  // the previous round's push phase
         if (!err) err = team.rd32(&st->error);
-        const uint32_t ncand = team.rd32(&st->cand_count[r3]);
         ins_total += team.rd64(&st->ins[r3]);
+        if (!err && ins_total > m.max_inserted) err = ST_HASH_FULL;
         const bool pause = ins_total > m.grow_at;
         round += 1;
         if (err) {
@@ -690,9 +792,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
             st->round_min[a] = kInfCost;
             st->goal_min[a] = kInfCost;
             st->ins[a] = 0;
-            st->cand_count[a] = 0;
             st->err[a] = 0;
-            st->err2[(r3 + 1) % 3] = 0;  // last read by this round's predecessor's decision
         }
         // This CTA's share of the round's candidates is every C-th one (a
         // contiguous chunk would hold the successors of a few warps' pops,
@@ -700,9 +800,35 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         // team's heaps of it).  All threads check a part of the share: a
         // candidate is the slot's winner iff the slot's g still equals its g;
         // winners write prev/aux and are staged for their heap's owner.
+        // The round's candidates are numbered region by region: offsets of the
+        // C regions (each thread sums `per` consecutive regions' counts).
+        const uint32_t per = (C + T - 1) / T, rb = tid * per, re = min(rb + per, C);
+        uint32_t mine = 0;
+        for (uint32_t r = rb; r < re; ++r) {
+            const uint32_t n = ldcg_u32(&half[(size_t)r * RR].slot);
+            roff[r] = n;
+            mine += n;
+        }
+        uint32_t ncand;
+        uint32_t off = block_excl_scan(mine, scratch, &ncand);
+        for (uint32_t r = rb; r < re; ++r) {
+            const uint32_t n = roff[r];
+            roff[r] = off;
+            off += n;
+        }
+        __syncthreads();
         const uint32_t nshare = ncand > cta ? (ncand - cta + C - 1) / C : 0u;
         for (uint32_t q = tid; q < nshare; q += T) {
-            const Cand c = load_cand(cand + cta + (size_t)C * q);
+            const uint32_t i = cta + C * q;
+            uint32_t lo = 0, hi = C - 1;  // the last region starting at or before i
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1) >> 1;
+                if (roff[mid] <= i)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            const Cand c = load_cand(half + (size_t)lo * RR + 1 + (i - roff[lo]));
             E e = prob.make_entry(c.f, c.g, c.slot);
             if (ldcg_u64(&m.tab[c.slot].g) == c.g) {
                 m.tab[c.slot].prev = c.parent;
@@ -724,12 +850,14 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                 ++nP;
             }
         }
-        base = (uint32_t)(((uint64_t)base + ncand) % H);
+        base = (uint32_t)(((uint64_t)base + nshare) % H);
         if (pause || it + 1 >= budget) break;
     }
 
     // Persist the resumable state: the buffers go into the heaps, then the
-    // sizes and the shared tops.
+    // sizes and the shared tops.  (The pushes use the sift scratch, which
+    // the last push phase's staging shares: wait for every owner first.)
+    __syncthreads();
     if (owner && status == ST_RUNNING) {
         while (bn > 0) {
             if (hs + 1 > m.hcap) {

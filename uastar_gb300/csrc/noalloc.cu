@@ -52,7 +52,7 @@ constexpr uint32_t kHeapStride = 4672;
 constexpr size_t kOffState = 0;
 constexpr size_t kOffSizes = align256(kOffState + sizeof(TeamState));
 constexpr size_t kOffCand = align256(kOffSizes + kHeaps * sizeof(uint32_t));
-constexpr size_t kOffHeaps = align256(kOffCand + 2 * (size_t)kHeaps * GridProblem::kMoves * sizeof(Cand));
+constexpr size_t kOffHeaps = align256(kOffCand + cand_records<GridProblem>(kCtas, kHeapsPerCta) * sizeof(Cand));
 constexpr size_t kOffTable = align256(kOffHeaps + (size_t)kHeaps * kHeapStride * sizeof(GridEntry));
 constexpr size_t kScratchBytes = align256(kOffTable + kTableSlots * sizeof(Slot));
 
