@@ -237,6 +237,9 @@ typedef struct {
     int32_t heap_capacity;
     int32_t rounds_per_quantum; /* GA* rounds per persistent-kernel launch (0 -> 256) */
     double load_factor;
+    int32_t cluster_slots;    /* cap on 8-CTA slots for requests whose search outgrows one CTA
+                                 (0 -> as many as fit, -1 -> none) */
+    int32_t reserved;
 } uastar_serve_config;
 
 typedef struct {

@@ -60,8 +60,9 @@ def test_stream_results_equal_alone_and_in_mix(seng):
 
 
 def test_cancel_and_reject(seng):
-    seng.serve_start(hbm_budget_gb=0.5, slots=4, rounds_per_quantum=16)
-    big = WL.GridSpec(8000, 8000, 0.1, 1).instance()       # partition far above the budget
+    # 100 MB: the 8000^2 grid's 8 MB bitmap cannot fit its 5 MB arena
+    seng.serve_start(hbm_budget_gb=0.1, slots=4, rounds_per_quantum=16)
+    big = WL.GridSpec(8000, 8000, 0.1, 1).instance()
     late = WL.PuzzleSpec(4, 200, 3).instance()
     r_big = seng.serve_submit(big)
     r_late = seng.serve_submit(late, WL.E.now_s() + 30.0)  # not yet arrived
@@ -70,3 +71,30 @@ def test_cancel_and_reject(seng):
     seng.serve_stop(10.0)
     assert got[r_big]["status"] == L.REJECTED
     assert got[r_late]["status"] == L.CANCELLED
+
+
+def test_wide_searches_move_to_cluster_slots(seng):
+    # every request starts on a CTA slot; the 15-puzzles of 200-move walks
+    # keep their CTA's heaps saturated and restart on 8-CTA cluster slots
+    # (attempts 2); the large sparse grids have thin frontiers and stay.
+    # Both tiers' results equal the plain engine's.
+    specs = [WL.screened_grid(2100 + 100 * i, 2100 + 100 * i, 0.15, 40 + i, exact=True) for i in range(3)]
+    specs += [WL.PuzzleSpec(4, 200, 1000 + i) for i in range(4)]
+    specs += [WL.PuzzleSpec(4, 30 + 5 * i, 900 + i) for i in range(4)]
+    insts = [s.instance() for s in specs]
+    seng.serve_start(hbm_budget_gb=32.0, rounds_per_quantum=128)
+    ids = [seng.serve_submit(inst) for inst in insts]
+    got = drain(seng, len(ids), timeout=60)
+    seng.serve_stop(30.0)
+    assert len(got) == len(ids)
+    assert max(got[i]["attempts"] for i in ids) >= 2
+    for rid, spec, inst in zip(ids, specs, insts):
+        r = got[rid]
+        if isinstance(spec, WL.PuzzleSpec):
+            p = seng.puzzle_solve(4, inst.tiles)
+            assert r["status"] == L.OK and r["steps"] == p.steps
+        else:
+            p = seng.grid_solve(inst.words, spec.H, spec.W, spec.start, spec.goal)
+            assert r["status"] == L.OK and p.ok
+            assert (r["straight"], r["diagonal"]) == (p.straight, p.diagonal)
+            assert float_equal(r["cost"], p.cost)

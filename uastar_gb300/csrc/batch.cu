@@ -31,6 +31,7 @@
 #include "ga_device.cuh"
 #include "ga_problems.cuh"
 #include "ga_search.cuh"
+#include "ga_grow.cuh"
 
 using namespace uastar;
 
@@ -50,6 +51,7 @@ struct InstDesc {
     uint64_t budget;      // batch: rounds before the instance gives up its team (0: the launch's)
     uint64_t key_off;     // batch: first path key of this instance in the key buffer
     uint64_t key_cap;     // batch: room for path keys
+    uint64_t grow_at;     // serving: pause the search when it has claimed this many slots (0: never)
 };
 
 struct InstOut {
@@ -127,12 +129,14 @@ __device__ uint32_t run_instance(const BatchArgs &a, const InstDesc &d, Team &te
                                reinterpret_cast<GridEntry *>(heaps),
                                own_geo ? d.heap_stride : a.stride_grid, own_geo ? d.heap_hcap : a.hcap_grid,
                                a.L_grid, hs, cand, d.max_rounds};
+        if (d.grow_at) m.grow_at = d.grow_at;
         return ga_search(prob, team, m, a.H, smem, budget);
     }
     SearchMem<PuzzleEntry> m{tab, slots - 1, (uint64_t)(slots * a.max_load), 4096u,
                              reinterpret_cast<PuzzleEntry *>(heaps),
                              own_geo ? d.heap_stride : a.stride_puzzle, own_geo ? d.heap_hcap : a.hcap_puzzle,
                              a.L_puzzle, hs, cand, d.max_rounds};
+    if (d.grow_at) m.grow_at = d.grow_at;
     if (d.n == 4) {
         PuzzleProblem<4> prob;
         prob.pdb = a.pdb4;
@@ -201,9 +205,9 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
             // a phase-2 error of the last round of a quantum is still in error2
             // an error of a parked search is reported by its next decision: report it now
             if (o.status == ST_RUNNING && st.error) o.status = st.error;
-            // batch: the region is reused by the next instance, so the path
-            // is read out now
-            if (!a.serving && o.status == ST_OK) o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap);
+            // the path is read out now (a batch region is reused by the
+            // team's next instance)
+            if (o.status == ST_OK) o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap);
             a.outs[i] = o;
             if (a.serving) a.states[i] = st;
         }
@@ -272,7 +276,7 @@ __global__ void __launch_bounds__(512, 1) k_batch_cluster(BatchArgs a) {
             o.t_end = globaltimer_ns();
             const uint32_t pend = ldcg_u32(&st->error);
             if (o.status == ST_RUNNING && pend) o.status = pend;
-            if (!a.serving && o.status == ST_OK) o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap);
+            if (o.status == ST_OK) o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap);
             a.outs[i] = o;
         }
         team.sync();
@@ -971,7 +975,6 @@ struct ServeReq {
     uint64_t mult = 1;            // dedup partition growth (overflow, promotion)
     uint32_t heap_mult = 1;       // heap slice growth after HEAP_OVERFLOW
     int attempts = 0;
-    bool large = false;           // runs on a cluster slot
     uastar_instance_result acc{};
 };
 
@@ -981,9 +984,10 @@ struct ServeSlot {
     uint64_t tab_off = 0, tab_n = 0, bm_off = 0, bm_n = 0, heap_off = 0, heap_n = 0;
 };
 
-// One kind of resident slot: single CTAs (small requests) or 8-CTA clusters
-// (large requests).  Each tier has its own quantum kernel and stream; the two
-// kernels run side by side.
+// One kind of resident slot: single CTAs (puzzles, small grids) or 8-CTA
+// clusters (large grids, and requests that outgrew a CTA).  Each tier has its
+// own quantum kernel and stream and is relaunched as soon as its previous
+// quantum has been retired, independently of the other tier.
 struct ServeTier {
     bool large = false;
     int nslots = 0;
@@ -991,12 +995,26 @@ struct ServeTier {
     std::vector<ServeSlot> slots;
     std::vector<InstDesc> descs;
     std::vector<InstOut> outs;
-    DevBuf d_descs, d_outs, d_states, d_hsize, d_cand, d_walk;
+    DevBuf d_descs, d_outs, d_states, d_hsize, d_cand, d_keys, d_walk, d_map;
+    uint64_t kcap = 0;  // path keys per slot (walked in the kernel)
     cudaStream_t stream = nullptr;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr, done = nullptr;
+    bool inflight = false;
+    std::vector<char> launched;  // slots that are part of the quantum in flight
     int resident() const {
         int n = 0;
         for (auto &sl : slots) n += sl.busy;
+        return n;
+    }
+    int free_slot() const {
+        for (int q = 0; q < nslots; ++q)
+            if (!slots[q].busy) return q;
+        return -1;
+    }
+    int extent() const {  // slots a launch must cover
+        int n = 0;
+        for (int q = 0; q < nslots; ++q)
+            if (slots[q].busy) n = q + 1;
         return n;
     }
 };
@@ -1005,7 +1023,7 @@ struct ServeState {
     uastar_engine *eng = nullptr;
     uastar_serve_config cfg{};
     ServeTier tier[2];  // 0 = CTA slots, 1 = cluster slots
-    uint64_t promote_rounds = 4096;
+    int capacity = 0;   // co-resident CTAs shared by both tiers' resident requests
     uint64_t heap_bytes = 0;
     std::thread th;
     std::mutex mu;
@@ -1038,9 +1056,14 @@ static void serve_complete(ServeState *S, ServeReq &r, int32_t status) {
     if (status == UASTAR_REJECTED) S->stats.rejected += 1;
 }
 
+// A request's first dedup partition: its estimate, but at most 2^20 slots
+// times its growth multiplier; the search grows it 4x in place whenever it
+// is half full (serve_grow), so admission reserves what a request has shown
+// it needs rather than what the largest like it might.
 static uint64_t serve_partition_slots(const ServeState *S, const ServeReq &r) {
     const double load = S->cfg.load_factor > 0 && S->cfg.load_factor < 1 ? S->cfg.load_factor : 0.5;
-    uint64_t slots = next_pow2_u64((uint64_t)((double)est_nodes(r.inst) * (double)r.mult / load));
+    uint64_t slots = next_pow2_u64((uint64_t)((double)est_nodes(r.inst) / load));
+    slots = std::min<uint64_t>(slots, 1ull << 20) * r.mult;
     return std::max<uint64_t>(slots, 1u << 12);
 }
 
@@ -1051,16 +1074,16 @@ static void serve_release(ServeState *S, ServeSlot &sl) {
 }
 
 // Try to place `r` in a free slot of tier `t`.  Returns 1 placed, 0 no room
-// now, -1 can never fit (completed as REJECTED by the caller).
+// now, -1 can never fit (completed as REJECTED by the caller).  A free slot
+// is not part of a running quantum, so this may run while the tier's kernel
+// is in flight: the partition clear and the bitmap copy queue behind it on
+// the tier's stream, and the descriptor is uploaded with the next launch.
 static int serve_admit(ServeState *S, ServeTier &t, ServeReq &r) {
     uastar_engine *eng = S->eng;
-    int free_slot = -1;
-    for (int q = 0; q < t.nslots; ++q)
-        if (!t.slots[q].busy) {
-            free_slot = q;
-            break;
-        }
-    if (free_slot < 0) return 0;
+    const int q = t.free_slot();
+    if (q < 0) return 0;
+    // both tiers' resident requests share the GPU's co-resident CTAs
+    if (S->tier[0].resident() + 8 * S->tier[1].resident() + (t.large ? 8 : 1) > S->capacity) return 0;
     const uint64_t tn = serve_partition_slots(S, r);
     const uint64_t bn = r.inst.kind == UASTAR_KIND_GRID ? r.words.size() + 2 : 0;
     BatchGeometry hgeo = t.geo;
@@ -1082,7 +1105,7 @@ static int serve_admit(ServeState *S, ServeTier &t, ServeReq &r) {
         if (bn) S->bm_alloc.release(boff, bn);
         return 0;
     }
-    ServeSlot &sl = t.slots[free_slot];
+    ServeSlot &sl = t.slots[q];
     sl.busy = true;
     sl.tab_off = toff;
     sl.tab_n = tn;
@@ -1103,6 +1126,9 @@ static int serve_admit(ServeState *S, ServeTier &t, ServeReq &r) {
     d.heap_off = hoff * 16;
     d.heap_stride = hstride;
     d.heap_hcap = hhcap;
+    d.key_off = (uint64_t)q * t.kcap;
+    d.key_cap = t.kcap;
+    d.grow_at = tn / 2;
     if (fill_ff_async(eng, S->tab.as<Slot>() + toff, tn * sizeof(Slot), t.stream) != UASTAR_OK) {
         S->loop_error = UASTAR_CUDA_ERROR;
         return 0;
@@ -1121,7 +1147,7 @@ static int serve_admit(ServeState *S, ServeTier &t, ServeReq &r) {
     } else {
         d.start_key = pack_board(d.n, sl.req.inst.tiles);
     }
-    t.descs[free_slot] = d;
+    t.descs[q] = d;
     return 1;
 }
 
@@ -1149,14 +1175,266 @@ static BatchArgs serve_args(ServeState *S, ServeTier &t) {
     a.L_puzzle = t.geo.L_puzzle;
     a.budget = (uint64_t)(S->cfg.rounds_per_quantum > 0 ? S->cfg.rounds_per_quantum : 256);
     a.serving = 1;
+    a.keys = t.d_keys.as<unsigned long long>();
     return a;
+}
+
+// One quantum of tier t: descriptors up, kernel, results down; `done` marks
+// the end.
+static cudaError_t serve_launch(ServeState *S, ServeTier &t) {
+    cudaError_t e;
+    const int n = t.extent();
+    if ((e = cudaMemcpyAsync(t.d_descs.p, t.descs.data(), n * sizeof(InstDesc), cudaMemcpyHostToDevice,
+                             t.stream)) != cudaSuccess)
+        return e;
+    BatchArgs a = serve_args(S, t);
+    cudaEventRecord(t.e0, t.stream);
+    if (t.large) {
+        cudaLaunchConfig_t lc = {};
+        cudaLaunchAttribute lat[1];
+        lat[0].id = cudaLaunchAttributeClusterDimension;
+        lat[0].val.clusterDim.x = 8;
+        lat[0].val.clusterDim.y = 1;
+        lat[0].val.clusterDim.z = 1;
+        lc.gridDim = dim3((unsigned)(n * 8));
+        lc.blockDim = dim3((unsigned)t.geo.T);
+        lc.dynamicSmemBytes = t.geo.smem;
+        lc.stream = t.stream;
+        lc.attrs = lat;
+        lc.numAttrs = 1;
+        e = cudaLaunchKernelEx(&lc, k_batch_cluster, a);
+    } else {
+        k_batch<<<n, t.geo.T, t.geo.smem, t.stream>>>(a);
+        e = cudaGetLastError();
+    }
+    S->eng->launches++;
+    if (e != cudaSuccess) return e;
+    cudaEventRecord(t.e1, t.stream);
+    if ((e = cudaMemcpyAsync(t.outs.data(), t.d_outs.p, n * sizeof(InstOut), cudaMemcpyDeviceToHost,
+                             t.stream)) != cudaSuccess)
+        return e;
+    if ((e = cudaEventRecord(t.done, t.stream)) != cudaSuccess) return e;
+    t.inflight = true;
+    t.launched.assign(t.nslots, 0);
+    for (int q = 0; q < t.nslots; ++q) t.launched[q] = t.slots[q].busy;
+    return cudaSuccess;
+}
+
+// Reads a solved slot's path (goal -> start keys) into `keys`.
+static cudaError_t serve_path(ServeState *S, ServeTier &t, int q, std::vector<unsigned long long> &keys) {
+    const InstOut &o = t.outs[q];
+    const ServeSlot &sl = t.slots[q];
+    cudaError_t e;
+    if (o.path_len <= t.kcap) {
+        keys.resize(o.path_len);
+        if (o.path_len && (e = cudaMemcpyAsync(keys.data(), t.d_keys.as<unsigned long long>() + (size_t)q * t.kcap,
+                                               o.path_len * 8, cudaMemcpyDeviceToHost, t.stream)) != cudaSuccess)
+            return e;
+        return cudaStreamSynchronize(t.stream);
+    }
+    // longer than a slot's key room (a maze): walk it again into a buffer
+    // sized for the whole grid
+    const uint64_t cap = sl.req.inst.kind == UASTAR_KIND_GRID ? (uint64_t)sl.req.inst.H * sl.req.inst.W + 1 : 4096;
+    if ((e = t.d_walk.ensure(cap * 8 + 64)) != cudaSuccess) return e;
+    unsigned long long *d_keys = t.d_walk.as<unsigned long long>();
+    uint64_t *d_off = reinterpret_cast<uint64_t *>(d_keys + cap);
+    uint64_t *d_cap = d_off + 1;
+    unsigned long long *d_len = reinterpret_cast<unsigned long long *>(d_cap + 1);
+    uint32_t *d_which = reinterpret_cast<uint32_t *>(d_len + 1);
+    const uint64_t zero = 0;
+    const uint32_t which = (uint32_t)q;
+    cudaMemcpyAsync(d_off, &zero, 8, cudaMemcpyHostToDevice, t.stream);
+    cudaMemcpyAsync(d_cap, &cap, 8, cudaMemcpyHostToDevice, t.stream);
+    cudaMemcpyAsync(d_which, &which, 4, cudaMemcpyHostToDevice, t.stream);
+    k_batch_walk<<<1, 32, 0, t.stream>>>(t.d_descs.as<InstDesc>(), t.d_outs.as<InstOut>(), d_which, 1u,
+                                         S->tab.as<Slot>(), d_keys, d_off, d_cap, d_len);
+    S->eng->launches++;
+    unsigned long long len = 0;
+    cudaMemcpyAsync(&len, d_len, 8, cudaMemcpyDeviceToHost, t.stream);
+    if ((e = cudaStreamSynchronize(t.stream)) != cudaSuccess) return e;
+    if (len > cap) len = 0;
+    keys.resize(len);
+    if (len && (e = cudaMemcpyAsync(keys.data(), d_keys, len * 8, cudaMemcpyDeviceToHost, t.stream)) != cudaSuccess)
+        return e;
+    return cudaStreamSynchronize(t.stream);
+}
+
+// Checks a solved request's path on the host and fills its cost fields;
+// returns the status to report.
+static int32_t serve_finish_ok(ServeReq &r, const InstOut &o, const std::vector<unsigned long long> &kk) {
+    const auto &in = r.inst;
+    const uint64_t len = kk.size();
+    if (len == 0) return UASTAR_ARENA_FULL;
+    if (in.kind == UASTAR_KIND_GRID) {
+        r.acc.straight = (int64_t)(o.goal_best >> 32);
+        r.acc.diagonal = (int64_t)(o.goal_best & 0xffffffffu);
+        std::vector<int32_t> path(len);
+        for (uint64_t u = 0; u < len; ++u) path[u] = (int32_t)kk[len - 1 - u];
+        int64_t a2 = 0, b2 = 0;
+        float fc = 0;
+        if (uastar_validate_grid_path(r.words.data(), in.H, in.W, in.sx, in.sy, in.ex, in.ey, path.data(),
+                                      (int64_t)len, &a2, &b2, &fc) != UASTAR_OK ||
+            a2 != r.acc.straight || b2 != r.acc.diagonal)
+            return UASTAR_CUDA_ERROR;
+        r.acc.cost = fc;
+        return UASTAR_OK;
+    }
+    r.acc.steps = (int32_t)o.goal_best;
+    std::vector<int32_t> moves;
+    auto blank = [&](uint64_t k) {
+        for (int c = 0; c < in.n * in.n; ++c)
+            if (((k >> (4 * c)) & 15) == 0) return c;
+        return -1;
+    };
+    for (uint64_t u = len - 1; u >= 1; --u) {
+        const int pb = blank(kk[u]), cb = blank(kk[u - 1]);
+        moves.push_back(cb - pb == in.n ? 0 : cb - pb == -in.n ? 1 : cb - pb == 1 ? 2 : 3);
+    }
+    if ((int64_t)moves.size() != r.acc.steps ||
+        uastar_validate_puzzle_moves(in.n, in.tiles, moves.data(), (int64_t)moves.size()) != UASTAR_OK)
+        return UASTAR_CUDA_ERROR;
+    return UASTAR_OK;
+}
+
+// Move slot q's paused search (it passed grow_at) to a partition 4x larger:
+// the old one is rehashed into the new on the tier's stream (slots, prev
+// links, heap entries, goal slot), then released.  Without room it carries
+// on in place up to the table's load limit.
+static void serve_grow(ServeState *S, ServeTier &t, int q) {
+    uastar_engine *eng = S->eng;
+    ServeSlot &sl = t.slots[q];
+    InstDesc &d = t.descs[q];
+    const uint64_t old_n = 1ull << d.log2_slots, new_n = old_n * 4;
+    uint64_t noff = 0;
+    if (new_n > (1ull << 32) || !S->tab_alloc.alloc(new_n, 4, &noff)) {
+        d.grow_at = 0;
+        return;
+    }
+    if (t.d_map.ensure(old_n * 4) != cudaSuccess) {
+        S->tab_alloc.release(noff, new_n);
+        d.grow_at = 0;
+        return;
+    }
+    Slot *src = S->tab.as<Slot>() + d.tab_off, *dst = S->tab.as<Slot>() + noff;
+    uint32_t *map = t.d_map.as<uint32_t>();
+    const int blocks = std::max(1, eng->sms * 4);
+    const uint32_t per = t.large ? 8u : 1u;
+    const uint32_t k = t.geo.H * per;
+    uint32_t *hsize = t.d_hsize.as<uint32_t>() + (size_t)q * k;
+    TeamState *st = t.d_states.as<TeamState>() + q;
+    fill_ff_async(eng, dst, new_n * sizeof(Slot), t.stream);
+    k_grow_move<<<blocks, 256, 0, t.stream>>>(src, old_n, dst, new_n - 1, map);
+    k_grow_links<<<blocks, 256, 0, t.stream>>>(src, old_n, dst, map);
+    if (d.kind == UASTAR_KIND_GRID)
+        k_grow_heaps<GridProblem><<<blocks, 256, 0, t.stream>>>(
+            reinterpret_cast<GridEntry *>(S->heaps.as<uint8_t>() + d.heap_off), d.heap_stride, t.geo.L_grid, hsize,
+            k, map, st);
+    else
+        k_grow_heaps<PuzzleProblem<4>><<<blocks, 256, 0, t.stream>>>(
+            reinterpret_cast<PuzzleEntry *>(S->heaps.as<uint8_t>() + d.heap_off), d.heap_stride, t.geo.L_puzzle,
+            hsize, k, map, st);
+    eng->launches += 4;
+    // the old range may be handed out (and cleared on another stream) once released
+    if (cudaStreamSynchronize(t.stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+        S->loop_error = UASTAR_CUDA_ERROR;
+        return;
+    }
+    S->tab_alloc.release(sl.tab_off, sl.tab_n);
+    sl.tab_off = noff;
+    sl.tab_n = new_n;
+    d.tab_off = noff;
+    d.log2_slots += 2;
+    d.grow_at = new_n / 2;
+}
+
+// Retire tier t's finished quantum: completed requests report; one that
+// overflows its CTA slot restarts on a cluster slot with more space, one that
+// overflows a cluster slot retries there with more.  While the GPU has idle
+// CTAs and nothing is waiting (`spare`), a request that keeps its CTA's heaps
+// saturated (a wide frontier, which more heaps would cover in fewer rounds)
+// also moves to a cluster slot, trading throughput for its latency; under
+// load every request stays on one CTA, the most work per CTA.  A grid with a
+// thin frontier never moves: its rounds are bounded by its path length,
+// which a cluster would not shorten.
+static void serve_retire(ServeState *S, ServeTier &t, std::deque<ServeReq> &to_large, bool spare) {
+    ServeTier &large = S->tier[1];
+    float ms = 0;
+    cudaEventElapsedTime(&ms, t.e0, t.e1);
+    S->stats.quanta += 1;
+    S->stats.busy_ms += ms;
+    std::vector<unsigned long long> keys;
+    for (int q = 0; q < t.nslots; ++q) {
+        ServeSlot &sl = t.slots[q];
+        if (!sl.busy || !t.launched[q]) continue;  // admitted while the quantum ran
+        t.descs[q].fresh = 0;
+        const InstOut &o = t.outs[q];
+        ServeReq &r = sl.req;
+        if (o.status == ST_RUNNING) {
+            const bool saturated = o.rounds >= 1024 && (double)o.expanded >= 0.5 * t.geo.H * (double)o.rounds;
+            if (!t.large && saturated && spare && large.nslots > 0 && to_large.empty()) {
+                r.acc.expanded += (int64_t)o.expanded;
+                r.acc.generated += (int64_t)o.generated;
+                r.acc.rounds += (int64_t)o.rounds;
+                r.mult = std::max<uint64_t>(r.mult * 4, 4);
+                serve_release(S, sl);
+                to_large.push_back(std::move(r));
+                sl = ServeSlot();
+                t.descs[q].kind = 0;
+            } else if (t.descs[q].grow_at && o.inserted > t.descs[q].grow_at) {
+                serve_grow(S, t, q);
+                if (S->loop_error) return;
+            }
+            continue;
+        }
+        r.acc.device_ms = (double)(o.t_end - o.t_start) * 1e-6;
+        r.acc.expanded += (int64_t)o.expanded;
+        r.acc.generated += (int64_t)o.generated;
+        r.acc.rounds += (int64_t)o.rounds;
+        int32_t status = (int32_t)o.status;
+        if (status == ST_OK) {
+            if (serve_path(S, t, q, keys) != cudaSuccess) {
+                S->loop_error = UASTAR_CUDA_ERROR;
+                return;
+            }
+            status = serve_finish_ok(r, o, keys);
+        }
+        serve_release(S, sl);
+        t.descs[q].kind = 0;
+        if ((status == ST_HASH_FULL || status == ST_HEAP_OVERFLOW) && r.attempts < 8) {
+            if (status == ST_HASH_FULL) r.mult = std::max<uint64_t>(r.mult * (t.large ? 4 : 16), 16);
+            if (status == ST_HEAP_OVERFLOW) r.heap_mult *= t.large ? 16 : 2;
+            if (large.nslots > 0) {
+                if (t.large)
+                    to_large.push_front(std::move(r));
+                else
+                    to_large.push_back(std::move(r));
+                sl = ServeSlot();
+                continue;
+            }
+        }
+        if ((status == ST_HASH_FULL || status == ST_HEAP_OVERFLOW) && r.attempts < 8 && large.nslots == 0) {
+            // no cluster tier: retry on a CTA slot with the larger space
+            std::lock_guard<std::mutex> lk(S->mu);
+            S->incoming.push_front(std::move(r));
+            sl = ServeSlot();
+            continue;
+        }
+        serve_complete(S, r, status);
+        sl = ServeSlot();
+    }
 }
 
 static void serve_loop(ServeState *S) {
     uastar_engine *eng = S->eng;
     cudaSetDevice(eng->device);
+    // UASTAR_DEBUG: one line per second (quanta and kernel time per tier,
+    // residency, queues)
+    double log_t = uastar_now_s();
+    int64_t log_q[2] = {0, 0};
+    double log_ms[2] = {0, 0};
     std::vector<ServeReq> pending;   // arrived or future requests, sorted by arrival
-    std::deque<ServeReq> promoted;   // requests waiting for a cluster slot
+    std::deque<ServeReq> to_large;   // requests waiting for a cluster slot
+    ServeTier &small = S->tier[0], &large = S->tier[1];
     cudaError_t e;
     auto fail = [&](cudaError_t err, const char *what) {
         fail_cuda(eng, err, what);
@@ -1166,15 +1444,18 @@ static void serve_loop(ServeState *S) {
         // 1. intake and cancellation
         {
             std::unique_lock<std::mutex> lk(S->mu);
+            bool got = false;
             while (!S->incoming.empty()) {
                 pending.push_back(std::move(S->incoming.front()));
                 S->incoming.pop_front();
+                got = true;
             }
             std::vector<int64_t> cancels;
             cancels.swap(S->cancels);
             lk.unlock();
-            std::stable_sort(pending.begin(), pending.end(),
-                             [](const ServeReq &a, const ServeReq &b) { return a.arrival_s < b.arrival_s; });
+            if (got)
+                std::stable_sort(pending.begin(), pending.end(),
+                                 [](const ServeReq &a, const ServeReq &b) { return a.arrival_s < b.arrival_s; });
             for (int64_t cid : cancels) {
                 for (size_t i = 0; i < pending.size(); ++i)
                     if (pending[i].id == cid) {
@@ -1182,13 +1463,19 @@ static void serve_loop(ServeState *S) {
                         pending.erase(pending.begin() + i);
                         break;
                     }
-                for (size_t i = 0; i < promoted.size(); ++i)
-                    if (promoted[i].id == cid) {
-                        serve_complete(S, promoted[i], UASTAR_CANCELLED);
-                        promoted.erase(promoted.begin() + i);
+                for (size_t i = 0; i < to_large.size(); ++i)
+                    if (to_large[i].id == cid) {
+                        serve_complete(S, to_large[i], UASTAR_CANCELLED);
+                        to_large.erase(to_large.begin() + i);
                         break;
                     }
-                for (auto &t : S->tier)
+                // resident: only between quanta (its slot is not in a running kernel)
+                for (auto &t : S->tier) {
+                    if (t.inflight) {
+                        std::lock_guard<std::mutex> lk2(S->mu);
+                        S->cancels.push_back(cid);  // retry after this tier's quantum
+                        continue;
+                    }
                     for (int q = 0; q < t.nslots; ++q)
                         if (t.slots[q].busy && t.slots[q].req.id == cid) {
                             serve_complete(S, t.slots[q].req, UASTAR_CANCELLED);
@@ -1196,35 +1483,92 @@ static void serve_loop(ServeState *S) {
                             t.slots[q] = ServeSlot();
                             t.descs[q].kind = 0;
                         }
+                }
             }
         }
         if (S->loop_error) break;
-        // 2. admission: promoted requests into cluster slots, arrived ones into CTA slots
-        ServeTier &small = S->tier[0], &large = S->tier[1];
-        while (!promoted.empty() && large.nslots > 0) {
-            const int r = serve_admit(S, large, promoted.front());
+        // 2. retire finished quanta
+        for (auto &t : S->tier) {
+            if (!t.inflight) continue;
+            e = cudaEventQuery(t.done);
+            if (e == cudaErrorNotReady) continue;
+            if (e != cudaSuccess) {
+                fail(e, "serve quantum");
+                break;
+            }
+            t.inflight = false;
+            if (debug_log()) {
+                float ms = 0;
+                cudaEventElapsedTime(&ms, t.e0, t.e1);
+                log_q[t.large] += 1;
+                log_ms[t.large] += ms;
+            }
+            const bool spare = pending.empty() &&
+                               S->tier[0].resident() + 8 * (S->tier[1].resident() + 1) <= S->capacity;
+            serve_retire(S, t, to_large, spare);
+        }
+        if (S->loop_error) break;
+        // 3. admission: promoted requests take cluster slots, then arrived
+        //    requests take CTA slots in arrival order
+        while (!to_large.empty()) {
+            const int r = serve_admit(S, large, to_large.front());
             if (r == 0) break;
-            if (r < 0) serve_complete(S, promoted.front(), UASTAR_REJECTED);
-            promoted.pop_front();
+            if (r < 0) serve_complete(S, to_large.front(), UASTAR_REJECTED);
+            to_large.pop_front();
         }
         const double now = uastar_now_s();
-        size_t taken = 0;
-        for (; taken < pending.size(); ++taken) {
-            ServeReq &r = pending[taken];
-            if (r.arrival_s > now) break;
-            const int a = serve_admit(S, small, r);
-            if (a == 0) break;
-            if (a < 0) serve_complete(S, r, UASTAR_REJECTED);
+        {
+            std::vector<ServeReq> keep;
+            bool small_full = false;
+            for (auto &r : pending) {
+                if (r.arrival_s > now) {
+                    keep.push_back(std::move(r));
+                    continue;
+                }
+                if (small_full) {
+                    keep.push_back(std::move(r));
+                    continue;
+                }
+                const int a = serve_admit(S, small, r);
+                if (a == 0) {
+                    small_full = true;
+                    keep.push_back(std::move(r));
+                } else if (a < 0) {
+                    serve_complete(S, r, UASTAR_REJECTED);
+                }
+            }
+            pending.swap(keep);
         }
-        pending.erase(pending.begin(), pending.begin() + taken);
         const int rs = small.resident(), rl = large.resident();
+        if (debug_log() && uastar_now_s() - log_t >= 1.0) {
+            std::fprintf(stderr,
+                         "[uastar serve] CTA tier %lld quanta %.2f ms avg, %d/%d resident; cluster tier %lld quanta "
+                         "%.2f ms avg, %d/%d resident; waiting %zu (cluster queue %zu); completed %lld\n",
+                         (long long)log_q[0], log_q[0] ? log_ms[0] / log_q[0] : 0.0, rs, small.nslots,
+                         (long long)log_q[1], log_q[1] ? log_ms[1] / log_q[1] : 0.0, rl, large.nslots,
+                         pending.size(), to_large.size(), (long long)S->stats.completed);
+            log_t = uastar_now_s();
+            log_q[0] = log_q[1] = 0;
+            log_ms[0] = log_ms[1] = 0;
+        }
         S->stats.peak_resident = std::max(S->stats.peak_resident, rs + rl);
         S->stats.peak_budget_gb =
             std::max(S->stats.peak_budget_gb, ((double)S->tab_alloc.used() * sizeof(Slot) +
                                                (double)S->bm_alloc.used() * 8 + (double)S->heap_alloc.used() * 16) /
                                                   1e9);
         if (S->loop_error) break;
-        if (rs + rl == 0) {
+        // 4. launch every idle tier that has work: the cluster tier first
+        //    (its CTAs need whole GPCs)
+        for (int ti = 1; ti >= 0; --ti) {
+            ServeTier &t = S->tier[ti];
+            if (t.inflight || !t.nslots || !t.resident()) continue;
+            if ((e = serve_launch(S, t)) != cudaSuccess) {
+                fail(e, "serve launch");
+                break;
+            }
+        }
+        if (S->loop_error) break;
+        if (!small.inflight && !large.inflight) {
             std::unique_lock<std::mutex> lk(S->mu);
             if (S->abort_now || (S->draining && S->outstanding == 0)) break;
             double wait_s = 0.002;
@@ -1233,203 +1577,17 @@ static void serve_loop(ServeState *S) {
                 S->cv.wait_for(lk, std::chrono::duration<double>(wait_s));
             continue;
         }
-        // 3. one quantum: the cluster tier first (it needs whole GPCs), then the CTA tier
-        for (int ti = 1; ti >= 0; --ti) {
-            ServeTier &t = S->tier[ti];
-            if (!t.resident()) continue;
-            if ((e = cudaMemcpyAsync(t.d_descs.p, t.descs.data(), t.nslots * sizeof(InstDesc),
-                                     cudaMemcpyHostToDevice, t.stream)) != cudaSuccess) {
-                fail(e, "serve desc upload");
-                break;
-            }
-            BatchArgs a = serve_args(S, t);
-            cudaEventRecord(t.e0, t.stream);
-            if (t.large) {
-                cudaLaunchConfig_t lc = {};
-                cudaLaunchAttribute lat[1];
-                lat[0].id = cudaLaunchAttributeClusterDimension;
-                lat[0].val.clusterDim.x = 8;
-                lat[0].val.clusterDim.y = 1;
-                lat[0].val.clusterDim.z = 1;
-                lc.gridDim = dim3((unsigned)(t.nslots * 8));
-                lc.blockDim = dim3((unsigned)t.geo.T);
-                lc.dynamicSmemBytes = t.geo.smem;
-                lc.stream = t.stream;
-                lc.attrs = lat;
-                lc.numAttrs = 1;
-                e = cudaLaunchKernelEx(&lc, k_batch_cluster, a);
-            } else {
-                k_batch<<<t.nslots, t.geo.T, t.geo.smem, t.stream>>>(a);
-                e = cudaGetLastError();
-            }
-            eng->launches++;
-            cudaEventRecord(t.e1, t.stream);
-            if (e == cudaSuccess)
-                e = cudaMemcpyAsync(t.outs.data(), t.d_outs.p, t.nslots * sizeof(InstOut), cudaMemcpyDeviceToHost,
-                                    t.stream);
-            if (e != cudaSuccess) {
-                fail(e, "serve quantum");
-                break;
-            }
+        {
+            std::lock_guard<std::mutex> lk(S->mu);
+            if (S->abort_now) break;
         }
-        if (S->loop_error) break;
-        float qms = 0;
-        for (auto &t : S->tier) {
-            if (!t.resident()) continue;
-            if ((e = cudaStreamSynchronize(t.stream)) != cudaSuccess) {
-                fail(e, "serve quantum");
-                break;
-            }
-            float ms = 0;
-            cudaEventElapsedTime(&ms, t.e0, t.e1);
-            qms = std::max(qms, ms);
-        }
-        if (S->loop_error) break;
-        S->stats.quanta += 1;
-        S->stats.busy_ms += qms;
-        // 4. retire, promote or re-queue
-        for (int ti = 0; ti < 2; ++ti) {
-            ServeTier &t = S->tier[ti];
-            std::vector<uint32_t> which;
-            std::vector<uint64_t> koff, kcap;
-            uint64_t ktot = 0;
-            for (int q = 0; q < t.nslots; ++q) {
-                ServeSlot &sl = t.slots[q];
-                if (!sl.busy) continue;
-                t.descs[q].fresh = 0;
-                const InstOut &o = t.outs[q];
-                if (o.status == ST_RUNNING) {
-                    if (!t.large && o.rounds >= S->promote_rounds && large.nslots > 0) {
-                        // large after all: restart it on a cluster slot with more space
-                        ServeReq r = std::move(sl.req);
-                        r.acc.expanded += (int64_t)o.expanded;
-                        r.acc.rounds += (int64_t)o.rounds;
-                        r.mult = std::max<uint64_t>(r.mult * 16, 16);
-                        r.large = true;
-                        serve_release(S, sl);
-                        sl = ServeSlot();
-                        t.descs[q].kind = 0;
-                        promoted.push_back(std::move(r));
-                    }
-                    continue;
-                }
-                if (o.status == ST_OK) {
-                    const auto &in = sl.req.inst;
-                    which.push_back((uint32_t)q);
-                    koff.push_back(ktot);
-                    const uint64_t cap = in.kind == UASTAR_KIND_GRID ? 8ull * (in.H + in.W) + 64 : 512;
-                    kcap.push_back(cap);
-                    ktot += cap;
-                }
-            }
-            std::vector<unsigned long long> keys(ktot), lens(which.size());
-            if (!which.empty()) {
-                const size_t nw = which.size();
-                if ((e = t.d_walk.ensure(ktot * 8 + nw * 32 + 256)) != cudaSuccess) {
-                    fail(e, "serve walk alloc");
-                    break;
-                }
-                char *base = t.d_walk.as<char>();
-                unsigned long long *d_keys = reinterpret_cast<unsigned long long *>(base);
-                uint64_t *d_off = reinterpret_cast<uint64_t *>(base + ktot * 8);
-                uint64_t *d_cap = d_off + nw;
-                unsigned long long *d_len = reinterpret_cast<unsigned long long *>(d_cap + nw);
-                uint32_t *d_which = reinterpret_cast<uint32_t *>(d_len + nw);
-                cudaMemcpyAsync(d_off, koff.data(), nw * 8, cudaMemcpyHostToDevice, t.stream);
-                cudaMemcpyAsync(d_cap, kcap.data(), nw * 8, cudaMemcpyHostToDevice, t.stream);
-                cudaMemcpyAsync(d_which, which.data(), nw * 4, cudaMemcpyHostToDevice, t.stream);
-                k_batch_walk<<<(unsigned)((nw + 127) / 128), 128, 0, t.stream>>>(
-                    t.d_descs.as<InstDesc>(), t.d_outs.as<InstOut>(), d_which, (uint32_t)nw, S->tab.as<Slot>(),
-                    d_keys, d_off, d_cap, d_len);
-                eng->launches++;
-                cudaMemcpyAsync(lens.data(), d_len, nw * 8, cudaMemcpyDeviceToHost, t.stream);
-                cudaMemcpyAsync(keys.data(), d_keys, ktot * 8, cudaMemcpyDeviceToHost, t.stream);
-                if ((e = cudaStreamSynchronize(t.stream)) != cudaSuccess) {
-                    fail(e, "serve walk");
-                    break;
-                }
-            }
-            std::vector<int> walk_of(t.nslots, -1);
-            for (size_t w = 0; w < which.size(); ++w) walk_of[which[w]] = (int)w;
-            for (int q = 0; q < t.nslots; ++q) {
-                ServeSlot &sl = t.slots[q];
-                if (!sl.busy || t.outs[q].status == ST_RUNNING) continue;
-                const InstOut &o = t.outs[q];
-                ServeReq &r = sl.req;
-                r.acc.device_ms = (double)(o.t_end - o.t_start) * 1e-6;
-                r.acc.expanded += (int64_t)o.expanded;
-                r.acc.generated += (int64_t)o.generated;
-                r.acc.rounds += (int64_t)o.rounds;
-                int32_t status = (int32_t)o.status;
-                serve_release(S, sl);
-                t.descs[q].kind = 0;
-                if (status == ST_HASH_FULL || status == ST_HEAP_OVERFLOW) {
-                    if (!t.large && large.nslots > 0) {
-                        r.mult = std::max<uint64_t>(r.mult * 16, 16);  // promote to a cluster slot
-                        if (status == ST_HEAP_OVERFLOW) r.heap_mult *= 2;
-                        r.large = true;
-                        promoted.push_back(std::move(r));
-                        sl = ServeSlot();
-                        continue;
-                    }
-                    if (r.attempts < 8) {
-                        if (status == ST_HASH_FULL) r.mult *= 4;
-                        else r.heap_mult *= 16;
-                        if (r.large)
-                            promoted.push_front(std::move(r));
-                        else
-                            pending.insert(pending.begin(), std::move(r));
-                        sl = ServeSlot();
-                        continue;
-                    }
-                }
-                if (status == ST_OK) {
-                    const int w = walk_of[q];
-                    const uint64_t len = lens[w];
-                    const unsigned long long *kk = keys.data() + koff[w];
-                    const auto &in = r.inst;
-                    if (len > kcap[w]) {
-                        status = UASTAR_ARENA_FULL;
-                    } else if (in.kind == UASTAR_KIND_GRID) {
-                        r.acc.straight = (int64_t)(o.goal_best >> 32);
-                        r.acc.diagonal = (int64_t)(o.goal_best & 0xffffffffu);
-                        std::vector<int32_t> path(len);
-                        for (uint64_t u = 0; u < len; ++u) path[u] = (int32_t)kk[len - 1 - u];
-                        int64_t a2 = 0, b2 = 0;
-                        float fc = 0;
-                        if (uastar_validate_grid_path(r.words.data(), in.H, in.W, in.sx, in.sy, in.ex, in.ey,
-                                                      path.data(), (int64_t)len, &a2, &b2, &fc) != UASTAR_OK ||
-                            a2 != r.acc.straight || b2 != r.acc.diagonal)
-                            status = UASTAR_CUDA_ERROR;
-                        r.acc.cost = fc;
-                    } else {
-                        r.acc.steps = (int32_t)o.goal_best;
-                        std::vector<int32_t> moves;
-                        auto blank = [&](uint64_t k) {
-                            for (int c = 0; c < in.n * in.n; ++c)
-                                if (((k >> (4 * c)) & 15) == 0) return c;
-                            return -1;
-                        };
-                        for (uint64_t u = len - 1; u >= 1; --u) {
-                            const int pb = blank(kk[u]), cb = blank(kk[u - 1]);
-                            moves.push_back(cb - pb == in.n ? 0 : cb - pb == -in.n ? 1 : cb - pb == 1 ? 2 : 3);
-                        }
-                        if ((int64_t)moves.size() != r.acc.steps ||
-                            uastar_validate_puzzle_moves(in.n, in.tiles, moves.data(), (int64_t)moves.size()) !=
-                                UASTAR_OK)
-                            status = UASTAR_CUDA_ERROR;
-                    }
-                }
-                serve_complete(S, r, status);
-                sl = ServeSlot();
-            }
-            if (S->loop_error) break;
-        }
-        if (S->loop_error) break;
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
+    for (auto &t : S->tier)
+        if (t.stream) cudaStreamSynchronize(t.stream);
     // drain: anything left is reported as cancelled
     for (auto &r : pending) serve_complete(S, r, UASTAR_CANCELLED);
-    for (auto &r : promoted) serve_complete(S, r, UASTAR_CANCELLED);
+    for (auto &r : to_large) serve_complete(S, r, UASTAR_CANCELLED);
     for (auto &t : S->tier)
         for (auto &sl : t.slots)
             if (sl.busy) serve_complete(S, sl.req, UASTAR_CANCELLED);
@@ -1443,9 +1601,11 @@ static void serve_loop(ServeState *S) {
 
 static void serve_free(ServeState *S) {
     for (auto &t : S->tier) {
-        for (DevBuf *b : {&t.d_descs, &t.d_outs, &t.d_states, &t.d_hsize, &t.d_cand, &t.d_walk}) b->release();
+        for (DevBuf *b : {&t.d_descs, &t.d_outs, &t.d_states, &t.d_hsize, &t.d_cand, &t.d_keys, &t.d_walk, &t.d_map})
+            b->release();
         if (t.e0) cudaEventDestroy(t.e0);
         if (t.e1) cudaEventDestroy(t.e1);
+        if (t.done) cudaEventDestroy(t.done);
         if (t.stream) cudaStreamDestroy(t.stream);
     }
     for (DevBuf *b : {&S->tab, &S->bitmaps, &S->heaps}) b->release();
@@ -1482,15 +1642,18 @@ int32_t uastar_serve_start(uastar_engine *eng, const uastar_serve_config *cfg) {
     large.geo = small.geo;
     large.large = true;
     const int capacity = small.geo.ctas;  // co-resident CTAs of the quantum kernels
-    // Cluster slots: a quarter of the capacity (at least one 8-CTA cluster)
-    // unless the caller asked for fewer slots than one cluster.
+    S->capacity = capacity;
+    // Both tiers can hold up to the whole GPU; admission keeps their resident
+    // requests within the co-resident CTAs together.
     int nlarge = 0;
-    if (resolve_cluster_geometry(eng, 8, &large.geo) == UASTAR_OK)
-        nlarge = std::max(1, std::min(large.geo.ctas / 8, capacity / 8 / 4));
-    int nsmall = capacity - 8 * nlarge;
+    if (S->cfg.cluster_slots >= 0 && resolve_cluster_geometry(eng, 8, &large.geo) == UASTAR_OK) {
+        nlarge = std::max(1, large.geo.ctas / 8);
+        if (S->cfg.cluster_slots > 0) nlarge = std::min(nlarge, S->cfg.cluster_slots);
+    }
+    int nsmall = capacity;
     if (S->cfg.slots > 0) {
         nsmall = std::min(nsmall, S->cfg.slots);
-        if (S->cfg.slots < 8) nlarge = 0;
+        if (S->cfg.slots < 8 && S->cfg.cluster_slots <= 0) nlarge = 0;
     }
     small.nslots = std::max(1, nsmall);
     large.nslots = nlarge;
@@ -1522,7 +1685,10 @@ int32_t uastar_serve_start(uastar_engine *eng, const uastar_serve_config *cfg) {
         std::memset(t.descs.data(), 0, t.descs.size() * sizeof(InstDesc));
         t.outs.assign(t.nslots, InstOut());
         if (!t.nslots) continue;
-        if ((e = t.d_descs.ensure((size_t)t.nslots * sizeof(InstDesc))) != cudaSuccess ||
+        t.kcap = 65600;  // path keys per slot (2 (H + W) + 64 for grids up to 16384 x 16384)
+        if ((e = t.d_keys.ensure((size_t)t.nslots * t.kcap * 8)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&t.done, cudaEventDisableTiming)) != cudaSuccess ||
+            (e = t.d_descs.ensure((size_t)t.nslots * sizeof(InstDesc))) != cudaSuccess ||
             (e = t.d_outs.ensure((size_t)t.nslots * sizeof(InstOut))) != cudaSuccess ||
             (e = t.d_states.ensure((size_t)t.nslots * sizeof(TeamState))) != cudaSuccess ||
             (e = t.d_hsize.ensure(ctas * t.geo.H * 4)) != cudaSuccess ||

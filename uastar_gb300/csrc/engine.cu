@@ -14,6 +14,7 @@
 #include "ga_device.cuh"
 #include "ga_problems.cuh"
 #include "ga_search.cuh"
+#include "ga_grow.cuh"
 
 using namespace uastar;
 
@@ -33,68 +34,6 @@ __global__ void __launch_bounds__(512, 1) k_plain_search(P prob, SearchMem<typen
     extern __shared__ __align__(128) unsigned char smem[];
     GridTeam team{st, 0u, timeout_ns};
     ga_search<P>(prob, team, m, H, smem, ~0ull);
-}
-
-// ---- moving a paused search to a larger dedup table ----------------------
-// A paused search (ga_search returned ST_RUNNING at a round boundary) names
-// slots in three places: the slots' prev links, the heap entries and the
-// team's goal slot.  Growth re-inserts every occupied slot into the empty
-// larger table, recording old -> new in `map`, then rewrites all three.
-
-// Re-insert the occupied slots of `src` (n slots) into `dst` (mask + 1
-// empty slots).  Keys are unique, so an insert only races other keys for an
-// empty slot; prev is copied as is and rewritten by k_grow_links.
-__global__ void k_grow_move(const Slot *src, uint64_t n, Slot *dst, uint64_t mask, uint32_t *map) {
-    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
-        const uint4 a = __ldcg(reinterpret_cast<const uint4 *>(src + s));
-        const unsigned long long key = ((unsigned long long)a.y << 32) | a.x;
-        if (key == kEmptyKey) continue;
-        const uint4 b = __ldcg(reinterpret_cast<const uint4 *>(src + s) + 1);
-        uint64_t h = mix64(key) & mask;
-        for (uint64_t probe = 0; probe <= mask; ++probe) {
-            if (atomicCAS(&dst[h].key, kEmptyKey, key) == kEmptyKey) break;
-            h = (h + 1) & mask;
-        }
-        uint4 *d = reinterpret_cast<uint4 *>(dst + h);
-        d[0] = make_uint4(a.x, a.y, a.z, a.w);  // key, g
-        d[1] = b;                               // aux, prev (old index), pad
-        map[s] = (uint32_t)h;
-    }
-}
-
-__global__ void k_grow_links(const Slot *src, uint64_t n, Slot *dst, const uint32_t *map) {
-    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
-        if (__ldcg(&src[s].key) == kEmptyKey) continue;
-        const uint32_t p = __ldcg(&src[s].prev);
-        dst[map[s]].prev = p == kNone ? kNone : map[p];
-    }
-}
-
-// One warp per heap: entries 1..size, the saved shared top first (heap
-// indices <= 2^L - 1 at the head of the heap's block), then the bricks.
-template <class P>
-__global__ void k_grow_heaps(typename P::Entry *heaps, uint32_t stride, uint32_t L, const uint32_t *heap_size,
-                             uint32_t k, const uint32_t *map, TeamState *st) {
-    using E = typename P::Entry;
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t topn = (1u << L) - 1u;
-    for (uint32_t h = warp; h < k; h += nwarps) {
-        E *gblock = heaps + (size_t)h * stride;
-        const BrickHeap<P> bh{gblock + top_reserve<P>(L), nullptr, nullptr, L};
-        const uint32_t sz = heap_size[h];
-        for (uint32_t i = 1 + lane; i <= sz; i += 32) {
-            E *q = i <= topn ? gblock + i : bh.g + bh.off(i);
-            E e = P::load(q);
-            e.slot = map[e.slot];
-            P::store(q, e);
-        }
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        if (st->goal_slot != kNone) st->goal_slot = map[st->goal_slot];
-        st->barrier = 0;  // the next launch counts barriers from zero
-    }
 }
 
 // Walk the prev chain from the goal slot (one thread: a pointer chase).
