@@ -356,6 +356,25 @@ def section_c5(eng, args):
     return out
 
 
+def section_mb(eng, args):
+    """Memory-bounded mode on the hardest 15-puzzle of the mixed batch (63
+    moves, ~7.5e7 states when solved exactly): the returned length next to
+    the proven lower bound, for dedup tables capped at 2^20 .. 2^24 slots."""
+    from uastar_gb300 import workloads as WL
+    ensure_pdb(eng)
+    tiles = WL.mixed_1024()[127].tiles()
+    out = []
+    for log2 in (20, 22, 24):
+        r = eng.puzzle_solve_bounded(4, tiles, log2)
+        out.append({"max_table_slots": 1 << log2, "table_mb": (1 << log2) * 32 >> 20, "status": r["status"],
+                    "steps": r["steps"], "lower_bound": r["lower_bound"], "segments": r["segments"],
+                    "expanded": r["expanded"], "solve_ms": round(r["solve_ms"], 1)})
+    opt = eng.puzzle_solve(4, tiles)
+    for row in out:
+        row["optimal_steps"] = opt.steps
+    return out
+
+
 # ------------------------------------------------------------ reference arm
 def run_reference(args, rank, world):
     if rank != 0:
@@ -401,7 +420,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--headline-only", action="store_true")
-    ap.add_argument("--sections", default="c3,c4,c5")
+    ap.add_argument("--sections", default="c3,c4,c5,mb")
     ap.add_argument("--cpu-cap", type=int, default=12_000_000)
     ap.add_argument("--ref-cap", type=int, default=3_000_000)
     ap.add_argument("--c3-count", type=int, default=100)
@@ -440,11 +459,12 @@ def main():
             from uastar_gb300 import Engine
             with Engine(local_rank) as deng:
                 secs = [s for s in args.sections.split(",") if s]
-                for name, fn in [("c3", section_c3), ("c4", section_c4), ("c5", section_c5)]:
+                for name, fn in [("c3", section_c3), ("c4", section_c4), ("c5", section_c5), ("mb", section_mb)]:
                     if name in secs:
                         t0 = time.perf_counter()
                         try:
-                            key = {"c3": "puzzle15_x100", "c4": "mixed_1024_batched", "c5": "serving"}[name]
+                            key = {"c3": "puzzle15_x100", "c4": "mixed_1024_batched", "c5": "serving",
+                                   "mb": "memory_bounded_puzzle"}[name]
                             line[key] = fn(deng, args)
                         except Exception as exc:  # report, keep the headline
                             line[f"{name}_error"] = repr(exc)

@@ -161,6 +161,30 @@ int32_t uastar_puzzle_solve(uastar_engine *eng, int32_t n, const uint8_t *tiles,
  * GPU-kernel.cuh:462-509).  Returns the move count or -status. */
 int64_t uastar_puzzle_moves(uastar_engine *eng, int32_t *moves, int64_t cap);
 
+/* Memory-bounded solve for puzzles too large for the dedup table (the
+ * reference's README.md:30-34 describes such a mode; it has no code for it).
+ * The search runs in segments of exact GA* with the table capped at
+ * 2^max_log2_slots slots (32 B each).  A segment that fills the table pauses;
+ * the open list's minimum f is then a lower bound on the remaining optimum,
+ * the search commits to the open node holding it and the next segment starts
+ * there.  The heuristic stays admissible throughout.  The result's steps are
+ * the returned solution's length, lower_bound the first segment's bound on
+ * the optimum (equal to steps when one segment sufficed: the solution is
+ * then optimal).  Moves via uastar_puzzle_moves. */
+typedef struct {
+    int32_t status;
+    int32_t steps;            /* moves of the returned solution */
+    int32_t lower_bound;      /* proven lower bound on the optimal move count */
+    int32_t segments;         /* exact searches run; 1 = the solution is optimal */
+    int64_t expanded;
+    int64_t generated;
+    double kernel_ms;
+    double solve_ms;
+} uastar_bounded_result;
+
+int32_t uastar_puzzle_solve_bounded(uastar_engine *eng, int32_t n, const uint8_t *tiles, int32_t max_log2_slots,
+                                    uastar_bounded_result *out);
+
 /* ---- batched persistent engine (many instances per launch) ----------- */
 enum { UASTAR_KIND_GRID = 1, UASTAR_KIND_PUZZLE = 2 };
 

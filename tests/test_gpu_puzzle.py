@@ -126,3 +126,24 @@ def test_table_grows_in_place_hard_puzzle(peng):
     assert r.table_grows >= 2
     assert r.table_used > (1 << 22)
     assert E.validate_puzzle_moves(4, tiles, peng.puzzle_moves())
+
+
+def test_memory_bounded_mode(peng):
+    """Bounded mode: with room to spare one exact segment (the optimum, its
+    own lower bound); with the table capped far below the search's needs
+    several segments, a valid solution no shorter than the reference's
+    optimum, and a lower bound no higher than it."""
+    rows = golden("puzzle_c3.json")
+    row = rows[0]
+    r = peng.puzzle_solve_bounded(4, row["tiles"], 28)
+    assert r["status"] == L.OK and r["segments"] == 1
+    assert r["steps"] == r["lower_bound"] == row["ref"]["steps"]
+    hard = golden("mixed_c4.json")[127]  # 63 moves, ~7.5e7 states
+    tiles = E.gen_puzzle(hard["seed"], 4, hard["walk"])
+    r = peng.puzzle_solve_bounded(4, tiles, 20)  # 2^20 slots
+    opt = hard["ref"]["steps"]
+    assert r["status"] == L.OK and r["segments"] > 1
+    assert r["lower_bound"] <= opt <= r["steps"]
+    assert r["lower_bound"] > 40
+    mv = peng.puzzle_moves()
+    assert len(mv) == r["steps"] and E.validate_puzzle_moves(4, tiles, mv)

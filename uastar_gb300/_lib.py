@@ -45,6 +45,11 @@ class PuzzleResult(C.Structure):
                 ("table_grows", C.c_int32), ("reserved", C.c_int32)]
 
 
+class BoundedResult(C.Structure):
+    _fields_ = [("status", C.c_int32), ("steps", C.c_int32), ("lower_bound", C.c_int32), ("segments", C.c_int32),
+                ("expanded", C.c_int64), ("generated", C.c_int64), ("kernel_ms", C.c_double), ("solve_ms", C.c_double)]
+
+
 class Instance(C.Structure):
     _fields_ = [("kind", C.c_int32), ("n", C.c_int32), ("H", C.c_int32), ("W", C.c_int32),
                 ("sx", C.c_int32), ("sy", C.c_int32), ("ex", C.c_int32), ("ey", C.c_int32),
@@ -120,6 +125,7 @@ SIGNATURES = [
     ("uastar_pdb_fetch", C.c_int32, [_P, C.c_int32, _U8P, C.c_int64]),
     ("uastar_puzzle_solve", C.c_int32, [_P, C.c_int32, _U8P, C.POINTER(PuzzleResult)]),
     ("uastar_puzzle_moves", C.c_int64, [_P, _I32P, C.c_int64]),
+    ("uastar_puzzle_solve_bounded", C.c_int32, [_P, C.c_int32, _U8P, C.c_int32, C.POINTER(BoundedResult)]),
     ("uastar_batch_solve", C.c_int32, [_P, C.POINTER(Instance), C.c_int32, C.POINTER(BatchConfig),
                                        C.POINTER(InstanceResult), C.POINTER(BatchStats)]),
     ("uastar_autotune", C.c_int32, [_P, C.POINTER(Instance), C.c_int32, C.POINTER(BatchConfig)]),

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "engine_internal.h"
@@ -34,6 +35,29 @@ __global__ void __launch_bounds__(512, 1) k_plain_search(P prob, SearchMem<typen
     extern __shared__ __align__(128) unsigned char smem[];
     GridTeam team{st, 0u, timeout_ns};
     ga_search<P>(prob, team, m, H, smem, ~0ull);
+}
+
+// The best open node of a paused puzzle search: the minimum entry (least f,
+// then deepest) among the entries of the heaps' saved shared tops that are
+// current (their f still matches the node's g), as key << 32 | slot into
+// *best by atomicMin.  The heap roots are the per-heap minima, so this is the
+// open list's minimum unless every root near it is stale.
+template <int N>
+__global__ void k_best_open(PuzzleProblem<N> prob, SearchMem<PuzzleEntry> m, uint32_t k,
+                            unsigned long long *best) {
+    const uint32_t topn = (1u << m.L) - 1u;
+    const uint64_t total = (uint64_t)k * topn;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t h = (uint32_t)(t / topn), i = (uint32_t)(t % topn) + 1;
+        if (i > __ldcg(&m.heap_size[h])) continue;
+        const PuzzleEntry e = PuzzleProblem<N>::load(m.heaps + (size_t)h * m.stride + i);
+        uint64_t key, g;
+        uint32_t aux;
+        PuzzleProblem<N>::load_node(m.tab + e.slot, key, g, aux);
+        if (prob.f_of(key, g, aux) != PuzzleProblem<N>::entry_cost(e)) continue;  // stale
+        atomicMin(best, ((unsigned long long)e.key << 32) | e.slot);
+    }
 }
 
 // Walk the prev chain from the goal slot (one thread: a pointer chase).
@@ -104,6 +128,8 @@ struct PlainOut {
     double kernel_ms;  // all search launches of the solve
     uint64_t slots;    // final table size
     int grows;         // in-place table growths
+    SearchMem<PuzzleEntry> mem;  // the last attempt's memory (puzzle solves; used by the bounded mode)
+    uint32_t k;        // heaps
 };
 
 // Run one instance with the whole GPU as the team.  Grows the dedup table /
@@ -156,9 +182,12 @@ bool grow_table(uastar_engine *eng, SearchMem<typename P::Entry> &m, uint32_t k,
     return true;
 }
 
+// max_log2 > 0 caps the dedup table at 2^max_log2 slots (the memory-bounded
+// mode): a search that fills it pauses near its load limit at a round
+// boundary and returns with status ST_RUNNING, its heaps and table intact.
 template <class P>
 int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t stride_auto,
-                  PlainOut *out) {
+                  PlainOut *out, int max_log2 = 0) {
     using E = typename P::Entry;
     const uastar_config &c = eng->cfg;
     const uint32_t block = (uint32_t)c.block_threads;
@@ -167,6 +196,7 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
     const uint32_t nblocks = (plain_heaps<P>(c) + H - 1) / H;
     const uint32_t k = nblocks * H;
     int log2 = c.hash_log2_slots > 0 ? c.hash_log2_slots : log2_auto;
+    if (max_log2 > 0) log2 = std::min(log2, max_log2);
     uint32_t stride = c.heap_capacity > 0 ? next_pow2_u32((uint32_t)c.heap_capacity + 1) : stride_auto;
 
     // shared heap tops: as many levels as fit while the whole team stays
@@ -227,9 +257,13 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
         m.heap_size = eng->heap_size.as<uint32_t>();
         m.cand = eng->cand.as<Cand>();
         m.max_rounds = (uint64_t)c.max_rounds;
-        // an auto-sized table grows in place (x4) when half full
-        const bool auto_table = c.hash_log2_slots <= 0;
-        m.grow_at = auto_table ? slots / 2 : ~0ull;
+        // an auto-sized table grows in place (x4) when half full; at the cap
+        // the search pauses instead, two rounds' worth of inserts short of
+        // the load limit
+        const bool auto_table = c.hash_log2_slots <= 0 || max_log2 > 0;
+        const uint64_t full_at = m.max_inserted > 4ull * k * P::kMoves ? m.max_inserted - 4ull * k * P::kMoves : 0;
+        auto pause_point = [&](uint64_t n) { return max_log2 > 0 && n >= (1ull << max_log2) ? full_at : n / 2; };
+        m.grow_at = auto_table ? pause_point(slots) : ~0ull;
         TeamState *st = eng->team.as<TeamState>();
         uint64_t timeout_ns = (uint64_t)(c.wait_timeout_s * 1e9);
         P pr = prob;
@@ -250,10 +284,13 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
             cudaEventElapsedTime(&ms, eng->ev0, eng->ev1);
             out->kernel_ms += ms;
             if (out->st.status != ST_RUNNING) break;
-            // paused for growth
+            // paused: at the cap the caller takes over; otherwise grow
+            if (max_log2 > 0 && m.mask + 1 >= (1ull << max_log2)) break;
             if (grow_table<P>(eng, m, k, st)) {
                 out->grows += 1;
-                m.grow_at = (m.mask + 1) / 2;
+                const uint64_t n = m.mask + 1;
+                const uint64_t fa = m.max_inserted > 4ull * k * P::kMoves ? m.max_inserted - 4ull * k * P::kMoves : 0;
+                m.grow_at = max_log2 > 0 && n >= (1ull << max_log2) ? fa : n / 2;
             } else {
                 m.grow_at = ~0ull;  // no room: carry on up to the load limit
                 if ((e = cudaMemsetAsync(&st->barrier, 0, sizeof(uint32_t), eng->stream)) != cudaSuccess)
@@ -261,12 +298,15 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
             }
         }
         out->slots = m.mask + 1;
+        if constexpr (std::is_same<E, PuzzleEntry>::value) out->mem = m;
+        out->k = k;
         log2 = ceil_log2_u64(out->slots);
+        if (out->st.status == ST_RUNNING) break;  // paused at the cap
 
         const uint32_t s = out->st.status;
         size_t free_b = 0, total_b = 0;
         cudaMemGetInfo(&free_b, &total_b);
-        if (s == ST_HASH_FULL && auto_table && log2 < 31 &&
+        if (s == ST_HASH_FULL && auto_table && log2 < 31 && (max_log2 <= 0 || log2 + 2 <= max_log2) &&
             (out->slots * 4 * sizeof(Slot)) < free_b + eng->tab.bytes) {
             log2 += 2;
             continue;
@@ -460,6 +500,79 @@ int32_t puzzle_solve_n(uastar_engine *eng, const uint8_t *tiles, uastar_puzzle_r
     return run_plain(eng, prob, N == 3 ? 20 : 22, N == 3 ? 1024 : 16383, po);
 }
 
+// Moves (0..3, the reference's DX/DY order) between consecutive packed boards.
+void keys_to_moves(int n, const std::vector<uint64_t> &keys, std::vector<int32_t> *moves) {
+    auto blank = [n](uint64_t k) {
+        for (int c = 0; c < n * n; ++c)
+            if (((k >> (4 * c)) & 15) == 0) return c;
+        return -1;
+    };
+    for (size_t i = 1; i < keys.size(); ++i) {
+        const int pb = blank(keys[i - 1]), cb = blank(keys[i]);
+        moves->push_back(cb - pb == n ? 0 : cb - pb == -n ? 1 : cb - pb == 1 ? 2 : 3);
+    }
+}
+
+// Memory-bounded solve: segments of exact GA*, each with the table capped.
+// A segment that fills the table pauses; the open list's minimum f then is
+// a lower bound on the remaining optimum (admissible h: every optimal path
+// crosses the open list), the search commits to the open node holding it
+// (least f, deepest) and the next segment starts there.  The first segment's
+// bound is a lower bound on the whole puzzle's optimum.
+template <int N>
+int32_t puzzle_bounded_n(uastar_engine *eng, const uint8_t *tiles, int max_log2, uastar_bounded_result *out,
+                         std::vector<int32_t> *moves) {
+    uint8_t cur[16];
+    std::memcpy(cur, tiles, N * N);
+    cudaError_t e;
+    for (int seg = 0; seg < 256; ++seg) {
+        PuzzleProblem<N> prob;
+        prob.pdb = eng->pdb[N].as<uint8_t>();
+        prob.start = pack_board(N, cur);
+        prob.goal = PuzzleProblem<N>::goal_key();
+        PlainOut po;
+        int32_t rc = run_plain(eng, prob, std::min(N == 3 ? 20 : 22, max_log2), N == 3 ? 1024 : 16383, &po, max_log2);
+        if (rc) return rc;
+        out->segments = seg + 1;
+        out->expanded += (int64_t)po.st.expanded;
+        out->generated += (int64_t)po.st.generated;
+        out->kernel_ms += po.kernel_ms;
+        std::vector<uint64_t> keys;
+        if (po.st.status == ST_OK) {
+            if (seg == 0) out->lower_bound = (int32_t)po.st.goal_best;
+            if ((rc = walk_keys(eng, po.st.goal_slot, 4096, &keys))) return rc;
+            keys_to_moves(N, keys, moves);
+            return UASTAR_OK;
+        }
+        if (po.st.status != ST_RUNNING) return (int32_t)po.st.status;
+        // paused with the table full: commit to the best open node
+        if ((e = eng->walk.ensure(4096 * 8 + 64)) != cudaSuccess) return fail_cuda(eng, e, "alloc walk");
+        unsigned long long *d_best = eng->walk.as<unsigned long long>();
+        const unsigned long long none = ~0ull;
+        cudaMemcpyAsync(d_best, &none, 8, cudaMemcpyHostToDevice, eng->stream);
+        k_best_open<N><<<std::max(1, eng->sms * 4), 256, 0, eng->stream>>>(prob, po.mem, po.k, d_best);
+        eng->launches++;
+        unsigned long long best = ~0ull;
+        cudaMemcpyAsync(&best, d_best, 8, cudaMemcpyDeviceToHost, eng->stream);
+        if ((e = cudaStreamSynchronize(eng->stream)) != cudaSuccess) return fail_cuda(eng, e, "best open node");
+        if (best == ~0ull) {
+            eng->set_err("bounded search: no current open node at the memory bound");
+            return UASTAR_HASH_FULL;
+        }
+        const uint32_t f = (uint32_t)(best >> 48);  // entry key = f << 16 | (0xffff - g)
+        if (seg == 0) out->lower_bound = (int32_t)f;
+        if ((rc = walk_keys(eng, (uint32_t)best, 4096, &keys))) return rc;
+        if (keys.size() < 2) {
+            eng->set_err("bounded search: the best open node is the start");
+            return UASTAR_HASH_FULL;
+        }
+        keys_to_moves(N, keys, moves);
+        for (int c = 0; c < N * N; ++c) cur[c] = (uint8_t)((keys.back() >> (4 * c)) & 15);
+    }
+    eng->set_err("bounded search: segment limit reached");
+    return UASTAR_ITER_LIMIT;
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ C ABI ---
@@ -621,6 +734,49 @@ int32_t uastar_puzzle_solve(uastar_engine *eng, int32_t n, const uint8_t *tiles,
     } else if (st.status == ST_RUNNING) {
         eng->set_err("search kernel ended without a status");
         out->status = UASTAR_CUDA_ERROR;
+    }
+    out->solve_ms = now_ms() - t0;
+    return out->status;
+}
+
+int32_t uastar_puzzle_solve_bounded(uastar_engine *eng, int32_t n, const uint8_t *tiles, int32_t max_log2_slots,
+                                    uastar_bounded_result *out) {
+    if (!eng || !out) return UASTAR_BAD_INPUT;
+    const double t0 = now_ms();
+    std::memset(out, 0, sizeof(*out));
+    cudaSetDevice(eng->device);
+    eng->last_ok = false;
+    eng->path_cached = false;
+    eng->last_kind = UASTAR_KIND_PUZZLE;
+    if ((n != 3 && n != 4) || !tiles || !board_ok(n, tiles) || max_log2_slots < 16 || max_log2_slots > 31) {
+        eng->set_err("bounded solve: 3x3 or 4x4 board with tiles 0..n*n-1 once each, 16 <= max_log2_slots <= 31");
+        return out->status = UASTAR_BAD_INPUT;
+    }
+    if (!eng->pdb_ready[n]) {
+        eng->set_err("pattern database not resident: call uastar_pdb_build or uastar_pdb_load");
+        return out->status = UASTAR_BAD_INPUT;
+    }
+    if (!board_solvable(n, tiles)) {
+        out->status = UASTAR_NO_SOLUTION;
+        out->solve_ms = now_ms() - t0;
+        return out->status;
+    }
+    std::vector<int32_t> moves;
+    int32_t rc = n == 3 ? puzzle_bounded_n<3>(eng, tiles, max_log2_slots, out, &moves)
+                        : puzzle_bounded_n<4>(eng, tiles, max_log2_slots, out, &moves);
+    out->status = rc;
+    if (rc == UASTAR_OK) {
+        out->steps = (int32_t)moves.size();
+        if (uastar_validate_puzzle_moves(n, tiles, moves.data(), (int64_t)moves.size()) != UASTAR_OK) {
+            eng->set_err("bounded solve returned moves that fail host validation");
+            out->status = UASTAR_CUDA_ERROR;
+        } else {
+            eng->path = moves;
+            eng->last_ok = true;
+            eng->path_cached = true;
+            eng->last_n = n;
+            std::memcpy(eng->last_tiles, tiles, (size_t)n * n);
+        }
     }
     out->solve_ms = now_ms() - t0;
     return out->status;

@@ -304,6 +304,17 @@ class Engine:
         return PuzzleSolution(r.status, r.steps, r.expanded, r.generated, r.pushed, r.rounds, r.table_used,
                               r.kernel_ms, r.solve_ms, r.table_grows)
 
+    def puzzle_solve_bounded(self, n: int, tiles: Sequence[int], max_log2_slots: int) -> dict:
+        """Memory-bounded solve (dedup table capped at 2^max_log2_slots slots):
+        the returned solution's `steps`, a proven `lower_bound` on the optimum
+        and the number of exact `segments` (1: the solution is optimal)."""
+        t = np.ascontiguousarray(np.asarray(tiles, dtype=np.uint8))
+        r = L.BoundedResult()
+        self._lib.uastar_puzzle_solve_bounded(self._h, n, _u8p(t), max_log2_slots, C.byref(r))
+        if r.status in (L.CUDA_ERROR, L.BAD_INPUT, L.TIMEOUT):
+            raise EngineError(r.status, self.last_error)
+        return {k: getattr(r, k) for k, _ in L.BoundedResult._fields_}
+
     def puzzle_moves(self) -> list[int]:
         n = self._lib.uastar_puzzle_moves(self._h, None, 0)
         if n < 0:
