@@ -26,7 +26,8 @@ def main() -> None:
 
     if args.case in ("grid_1000", "grid_20000"):
         sp = WL.GRID_1000 if args.case == "grid_1000" else WL.GRID_20000
-        kw = {"hash_log2_slots": 28} if args.case == "grid_20000" else {}
+        # fixed tables: one search launch per solve (no in-place growth)
+        kw = {"hash_log2_slots": 28 if args.case == "grid_20000" else 22}
         words = sp.words()
         with Engine(0, heaps=8192, block_threads=256, threads_per_heap=4, **kw) as eng:
             for _ in range(args.repeat):
@@ -34,7 +35,7 @@ def main() -> None:
                 print(f"{args.case}: {r.straight}+{r.diagonal}*sqrt2 cost {r.cost:.4f} expanded {r.expanded} "
                       f"rounds {r.rounds} kernel {r.kernel_ms:.1f} ms", flush=True)
     elif args.case == "puzzle15":
-        with Engine(0) as eng:
+        with Engine(0, hash_log2_slots=25) as eng:  # fixed table: one launch per solve
             eng.pdb_build(4)
             for _ in range(args.repeat):
                 t0 = time.perf_counter()
