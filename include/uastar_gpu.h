@@ -140,11 +140,14 @@ typedef struct {
 /* Build the disjoint pattern databases of the n x n puzzle on the GPU by
  * backward breadth-first search and keep them resident (replaces
  * PatternDatabase::genDatabase, src/puzzle/database.cpp:37-84, called from
- * GPUPuzzleSolver::initialize, GPU-solver.cuh:130-138).  n = 3 or 4.
- * Partitions: n=3 {1..8}; n=4 {1,2,3,4,5,6,9,13} + {7,8,10,11,12,14,15}
- * (src/puzzle/CPU-solver.hpp:43-70).  build_ms (optional) gets the time. */
+ * GPUPuzzleSolver::initialize, GPU-solver.cuh:130-138).  n = 3, 4 or 5.
+ * Partitions: n=3 {1..8}; n=4 {1,2,3,4,5,6,9,13} + {7,8,10,11,12,14,15};
+ * n=5 {3,4,5,10,15,20} + {2,1,6,11,16,21} + {7,8,9,12,17,22} +
+ * {13,14,18,19,23,24} (src/puzzle/CPU-solver.hpp:43-102).  build_ms
+ * (optional) gets the time. */
 int32_t uastar_pdb_build(uastar_engine *eng, int32_t n, double *build_ms);
-/* Bytes of the concatenated tables for n (362,880 for n=3; 576,576,000 for n=4). */
+/* Bytes of the concatenated tables for n (362,880 for n=3; 576,576,000 for
+ * n=4; 510,048,000 for n=5). */
 int64_t uastar_pdb_bytes(int32_t n);
 /* Upload tables from the host in the reference's concatenated layout (table
  * t at the sum of the sizes of tables < t, GPU-solver.cuh:130-138) — e.g. the
@@ -153,7 +156,10 @@ int32_t uastar_pdb_load(uastar_engine *eng, int32_t n, const uint8_t *tables, in
 /* Copy the resident tables back (for the on-disk cache and byte checks). */
 int32_t uastar_pdb_fetch(uastar_engine *eng, int32_t n, uint8_t *out, int64_t bytes);
 /* Solve one board (replaces GPUPuzzleSolver<N>::solve, GPU-solver.cuh:197-274).
- * The tables for n must be resident (uastar_pdb_build or uastar_pdb_load). */
+ * n = 3, 4 or 5 (n*n bytes at tiles); the tables for n must be resident
+ * (uastar_pdb_build or uastar_pdb_load).  5x5 boards use 16-byte state keys
+ * (the reference's PuzzleStorage<5>, src/puzzle/storage.hpp:141-217, holds
+ * one in two words too); the batched and serving engines take 3x3 and 4x4. */
 int32_t uastar_puzzle_solve(uastar_engine *eng, int32_t n, const uint8_t *tiles,
                             uastar_puzzle_result *out);
 /* Blank moves of the last puzzle solve, start -> goal (replaces

@@ -92,7 +92,8 @@ def _i32(a):
 
 
 PARTITIONS = {3: [[1, 2, 3, 4, 5, 6, 7, 8]],
-              4: [[1, 2, 3, 4, 5, 6, 9, 13], [7, 8, 10, 11, 12, 14, 15]]}
+              4: [[1, 2, 3, 4, 5, 6, 9, 13], [7, 8, 10, 11, 12, 14, 15]],
+              5: [[3, 4, 5, 10, 15, 20], [2, 1, 6, 11, 16, 21], [7, 8, 9, 12, 17, 22], [13, 14, 18, 19, 23, 24]]}
 
 
 def pattern_size(n: int, tracked) -> int:

@@ -84,6 +84,8 @@ template <int N> static int run_pdb() {
     std::vector<std::vector<int>> tracked;
     if (N == 3) tracked = {{1, 2, 3, 4, 5, 6, 7, 8}};
     if (N == 4) tracked = {{1, 2, 3, 4, 5, 6, 9, 13}, {7, 8, 10, 11, 12, 14, 15}};
+    if (N == 5)
+        tracked = {{3, 4, 5, 10, 15, 20}, {2, 1, 6, 11, 16, 21}, {7, 8, 9, 12, 17, 22}, {13, 14, 18, 19, 23, 24}};
     for (auto &tr : tracked) {
         PatternDatabase pd(N, tr);
         std::vector<uint8_t> buf(pd.size());
@@ -113,10 +115,11 @@ int main(int argc, char **argv) {
         std::fprintf(stderr, "cannot enter %s\n", argv[3]);
         return 2;
     }
-    if (mode == "pdb") return n == 3 ? run_pdb<3>() : run_pdb<4>();
+    if (mode == "pdb") return n == 3 ? run_pdb<3>() : n == 4 ? run_pdb<4>() : run_pdb<5>();
     if (mode == "solve" && argc == 6)
         return n == 3 ? run_solve<3>(in_path.c_str(), out_path.c_str())
-                      : run_solve<4>(in_path.c_str(), out_path.c_str());
+               : n == 4 ? run_solve<4>(in_path.c_str(), out_path.c_str())
+                        : run_solve<5>(in_path.c_str(), out_path.c_str());
     std::fprintf(stderr, "bad mode\n");
     return 2;
 }

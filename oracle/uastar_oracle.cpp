@@ -399,7 +399,7 @@ typedef struct {
 } oracle_puzzle_result;
 
 // The pattern partitions of CPUPuzzleSolver<N>::initialize
-// (src/puzzle/CPU-solver.hpp:43-102) for N = 3 and 4.
+// (src/puzzle/CPU-solver.hpp:43-102) for N = 3, 4 and 5, in its tracked order.
 int oracle_puzzle_partition(int n, int *tracked_out, int *counts_out) {
     if (n == 3) {
         for (int i = 0; i < 8; ++i) tracked_out[i] = i + 1;
@@ -415,15 +415,22 @@ int oracle_puzzle_partition(int n, int *tracked_out, int *counts_out) {
         counts_out[1] = 7;
         return 2;
     }
+    if (n == 5) {
+        static const int t[24] = {3, 4, 5, 10, 15, 20, 2, 1, 6, 11, 16, 21, 7, 8, 9, 12, 17, 22, 13, 14, 18, 19, 23, 24};
+        std::memcpy(tracked_out, t, sizeof t);
+        for (int i = 0; i < 4; ++i) counts_out[i] = 6;
+        return 4;
+    }
     return 0;
 }
 
 // Restates CPUPuzzleSolver<N>::solve (src/puzzle/CPU-solver.hpp:154-231) with
 // its additive PDB heuristic computeHValue (:287-314) and lazy deletion of
 // heap entries whose fValue no longer matches the stored node (:162-165).
-// States are packed 4 bits per cell, cell (i,j) at bit 4*(i*n+j), the layout
-// of PuzzleStorage<3>/<4> (src/puzzle/storage.hpp:44-139; the last cell of a
-// 3x3 board is implied there and stored here, which changes no comparison).
+// States are packed 5 bits per cell, cell (i,j) at bit 5*(i*n+j) of a 128-bit
+// word (PuzzleStorage<3>/<4>/<5>, src/puzzle/storage.hpp:44-217, pack 4 or 5
+// bits per cell and leave one cell implied; only equality and hashing of the
+// packed state matter, and those agree).
 // pdbs[t] points at the table of pattern t, in partition order.
 // moves_out (optional, capacity moves_cap) receives blank moves 0..3 indexing
 // DX/DY (:237-262).
@@ -432,7 +439,7 @@ int oracle_puzzle_astar(int n, const uint8_t *tiles, const uint8_t *const *pdbs,
                         oracle_puzzle_result *res) {
     auto t0 = std::chrono::steady_clock::now();
     std::memset(res, 0, sizeof(*res));
-    int tracked[16], counts[4];
+    int tracked[32], counts[4];
     int npat = oracle_puzzle_partition(n, tracked, counts);
     if (npat == 0) return -1;
     oracle_pattern pats[4];
@@ -442,13 +449,20 @@ int oracle_puzzle_astar(int n, const uint8_t *tiles, const uint8_t *const *pdbs,
         off += counts[t];
     }
     const int nn = n * n;
+    typedef unsigned __int128 State;
     auto pack = [&](const uint8_t *c) {
-        uint64_t s = 0;
-        for (int i = 0; i < nn; ++i) s |= (uint64_t)c[i] << (4 * i);
+        State s = 0;
+        for (int i = 0; i < nn; ++i) s |= (State)c[i] << (5 * i);
         return s;
     };
-    auto unpack = [&](uint64_t s, uint8_t *c) {
-        for (int i = 0; i < nn; ++i) c[i] = (uint8_t)((s >> (4 * i)) & 15);
+    auto unpack = [&](State s, uint8_t *c) {
+        for (int i = 0; i < nn; ++i) c[i] = (uint8_t)((s >> (5 * i)) & 31);
+    };
+    struct StateHash {
+        size_t operator()(State s) const {
+            const uint64_t lo = (uint64_t)s, hi = (uint64_t)(s >> 64);
+            return std::hash<uint64_t>()(lo * 0x9E3779B97F4A7C15ull ^ hi);
+        }
     };
     auto hval = [&](const uint8_t *c) {
         int h = 0;
@@ -460,7 +474,7 @@ int oracle_puzzle_astar(int n, const uint8_t *tiles, const uint8_t *const *pdbs,
         return h;
     };
     struct Node {
-        uint64_t ps;
+        State ps;
         Node *prev;
         int f, g;
     };
@@ -470,10 +484,10 @@ int oracle_puzzle_astar(int n, const uint8_t *tiles, const uint8_t *const *pdbs,
         bool operator>(const Item &r) const { return f > r.f; }
     };
     std::priority_queue<Item, std::vector<Item>, std::greater<Item>> open;
-    std::unordered_map<uint64_t, Node *> closed;
+    std::unordered_map<State, Node *, StateHash> closed;
     uint8_t conf[64], goalc[64];
     for (int i = 0; i < nn; ++i) goalc[i] = (uint8_t)((i + 1) % nn);
-    const uint64_t target = pack(goalc);
+    const State target = pack(goalc);
     Node *root = new Node{pack(tiles), nullptr, 0, 0};
     root->f = hval(tiles);
     open.push({root->f, root});

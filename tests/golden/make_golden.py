@@ -4,7 +4,8 @@ oracle/Makefile.ref into oracle/_ref/) on the engine's seeded instances.
 
     python tests/golden/make_golden.py small c1      # seconds
     python tests/golden/make_golden.py c3 c4 c2      # minutes (c2 needs ~10 GB RAM)
-    python tests/golden/make_golden.py pdb           # after `ref_puzzle pdb 4` cached the tables
+    python tests/golden/make_golden.py pdb           # after `ref_puzzle pdb 4` (and 5) cached the tables
+    python tests/golden/make_golden.py p24small      # after `ref_puzzle pdb 5`
 
 Each part writes tests/golden/<part>.json.  Grid fixtures store the instance
 parameters and a sha256 of the generated bitmap (so a test can check that the
@@ -129,6 +130,16 @@ def part_p15small():
     (GOLDEN / "puzzle4_small.json").write_text(json.dumps(pz, indent=0))
 
 
+def part_p24small():
+    # 5x5 boards from short random walks: the reference's CPU A* (4 x 6-tile
+    # PDB, src/puzzle/CPU-solver.hpp:71-102) solves them in seconds
+    boards = [(5, E.gen_puzzle(200 + sd, 5, 8 + 4 * sd).tolist(), 200 + sd, 8 + 4 * sd) for sd in range(16)]
+    boards.append((5, list(range(1, 25)) + [0], None, 0))
+    res = ref_puzzle_parallel(5, [b[1] for b in boards], "small5", 4)
+    pz = [{"n": nn, "tiles": tiles, "seed": sd, "walk": walk, "ref": r} for (nn, tiles, sd, walk), r in zip(boards, res)]
+    (GOLDEN / "puzzle5_small.json").write_text(json.dumps(pz, indent=0))
+
+
 def ref_puzzle(n: int, boards, tag: str):
     inp, outp = WORK / f"{tag}.txt", WORK / f"{tag}.jsonl"
     inp.write_text("".join(" ".join(map(str, b)) + "\n" for b in boards))
@@ -203,7 +214,8 @@ def part_pdb():
     (GOLDEN / "pdb_sha256.json").write_text(json.dumps(out, indent=1))
 
 
-PARTS = {"small": part_small, "p15small": part_p15small, "c1": part_c1, "c2": part_c2, "c3": part_c3, "c4": part_c4, "pdb": part_pdb}
+PARTS = {"small": part_small, "p15small": part_p15small, "p24small": part_p24small, "c1": part_c1, "c2": part_c2,
+         "c3": part_c3, "c4": part_c4, "pdb": part_pdb}
 
 if __name__ == "__main__":
     if not (REF / "ref_grid").exists():

@@ -56,4 +56,5 @@ def test_build_info_and_pdb_sizes():
     assert b"sm_103a" in lib.uastar_build_info()
     assert lib.uastar_pdb_bytes(3) == 362880
     assert lib.uastar_pdb_bytes(4) == 16 * 15 * 14 * 13 * 12 * 11 * 10 * 9 + 16 * 15 * 14 * 13 * 12 * 11 * 10
-    assert lib.uastar_pdb_bytes(5) == 0
+    assert lib.uastar_pdb_bytes(5) == 4 * (25 * 24 * 23 * 22 * 21 * 20)
+    assert lib.uastar_pdb_bytes(6) == 0

@@ -27,6 +27,7 @@ def peng():
     with Engine(0) as eng:
         eng.pdb_build(3)
         eng.pdb_build(4)
+        eng.pdb_build(5)
         yield eng
 
 
@@ -147,3 +148,30 @@ def test_memory_bounded_mode(peng):
     assert r["lower_bound"] > 40
     mv = peng.puzzle_moves()
     assert len(mv) == r["steps"] and E.validate_puzzle_moves(4, tiles, mv)
+
+
+def test_pdb5_equals_reference_files(peng):
+    """The four 6-tile tables of the 5x5 puzzle, byte for byte the reference's
+    database_5_<tiles>.bin files (tracked order of CPU-solver.hpp:71-102)."""
+    sums = golden("pdb_sha256.json")
+    t = peng.pdb_fetch(5)
+    off = 0
+    for name in pdb_cache_names(5):
+        if name not in sums:
+            pytest.skip("24-puzzle reference tables not in the fixture")
+        n = sums[name]["bytes"]
+        assert hashlib.sha256(t[off:off + n].tobytes()).hexdigest() == sums[name]["sha256"], name
+        off += n
+    assert off == t.size
+
+
+def test_puzzle24_golden(peng):
+    """5x5 boards (16-byte state keys): exact optimal move counts of the
+    reference's CPU A*, moves that replay to the goal."""
+    for row in golden("puzzle5_small.json"):
+        if row["seed"] is not None:
+            assert E.gen_puzzle(row["seed"], 5, row["walk"]).tolist() == row["tiles"]
+        r = peng.puzzle_solve(5, row["tiles"])
+        assert r.ok and r.steps == row["ref"]["steps"], row
+        mv = peng.puzzle_moves()
+        assert len(mv) == r.steps and E.validate_puzzle_moves(5, row["tiles"], mv)

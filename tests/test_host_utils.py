@@ -43,6 +43,19 @@ def test_gen_puzzle_walk_properties():
         assert sorted(t.tolist()) == list(range(16))
     assert E.gen_puzzle(3, 4, 0).tolist() == list(range(1, 16)) + [0]
     assert (E.gen_puzzle(9, 3, 31) == E.gen_puzzle(9, 3, 31)).all()
+    for seed in range(5):
+        t = E.gen_puzzle(seed, 5, 60)
+        assert sorted(t.tolist()) == list(range(25))
+
+
+def test_puzzle24_walk_replays():
+    # a 5x5 walk undone by the reversed moves reaches the goal (validator on 25 cells)
+    t = E.gen_puzzle(7, 5, 0).tolist()
+    assert t == list(range(1, 25)) + [0]
+    assert E.validate_puzzle_moves(5, t, [])
+    assert E.validate_puzzle_moves(5, [1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 19, 20,
+                                       21, 22, 23, 0, 24], [2])
+    assert not E.validate_puzzle_moves(5, t, [0])  # off the board
 
 
 def test_pack_unpack_roundtrip():

@@ -1323,8 +1323,8 @@ static void serve_grow(ServeState *S, ServeTier &t, int q) {
     uint32_t *hsize = t.d_hsize.as<uint32_t>() + (size_t)q * k;
     TeamState *st = t.d_states.as<TeamState>() + q;
     fill_ff_async(eng, dst, new_n * sizeof(Slot), t.stream);
-    k_grow_move<<<blocks, 256, 0, t.stream>>>(src, old_n, dst, new_n - 1, map);
-    k_grow_links<<<blocks, 256, 0, t.stream>>>(src, old_n, dst, map);
+    k_grow_move<false><<<blocks, 256, 0, t.stream>>>(src, old_n, dst, new_n - 1, map);
+    k_grow_links<false><<<blocks, 256, 0, t.stream>>>(src, old_n, dst, map);
     if (d.kind == UASTAR_KIND_GRID)
         k_grow_heaps<GridProblem><<<blocks, 256, 0, t.stream>>>(
             reinterpret_cast<GridEntry *>(S->heaps.as<uint8_t>() + d.heap_off), d.heap_stride, t.geo.L_grid, hsize,

@@ -74,6 +74,22 @@ __global__ void k_walk(const Slot *tab, uint32_t goal_slot, unsigned long long *
     *len = (s != kNone) ? cap + 1 : n;
 }
 
+// The same walk for 16-byte keys: two words (lo, hi) per board.
+__global__ void k_walk_wide(const Slot *tab, uint32_t goal_slot, unsigned long long *keys, uint64_t cap,
+                            unsigned long long *len) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    uint32_t s = goal_slot;
+    uint64_t n = 0;
+    while (s != kNone && n < cap) {
+        const WideSlot *w = WideSlots::w(tab + s);
+        keys[2 * n] = __ldcg(&w->lo);
+        keys[2 * n + 1] = __ldcg(&w->hi);
+        ++n;
+        s = __ldcg(&w->prev);
+    }
+    *len = (s != kNone) ? cap + 1 : n;
+}
+
 int32_t fill_ff_async(uastar_engine *eng, void *p, size_t bytes, cudaStream_t stream) {
     const size_t n16 = bytes / 16;
     const int blocks = (int)std::min<size_t>((n16 + 255) / 256, (size_t)std::max(1, eng->sms * 8));
@@ -170,8 +186,8 @@ bool grow_table(uastar_engine *eng, SearchMem<typename P::Entry> &m, uint32_t k,
     const int blocks = std::max(1, eng->sms * 8);
     Slot *src = m.tab, *dst = eng->tab_next.as<Slot>();
     uint32_t *map = eng->grow_map.as<uint32_t>();
-    k_grow_move<<<blocks, 256, 0, eng->stream>>>(src, old_n, dst, new_n - 1, map);
-    k_grow_links<<<blocks, 256, 0, eng->stream>>>(src, old_n, dst, map);
+    k_grow_move<P::kWide><<<blocks, 256, 0, eng->stream>>>(src, old_n, dst, new_n - 1, map);
+    k_grow_links<P::kWide><<<blocks, 256, 0, eng->stream>>>(src, old_n, dst, map);
     k_grow_heaps<P><<<blocks, 256, 0, eng->stream>>>(m.heaps, m.stride, m.L, m.heap_size, k, map, st);
     eng->launches += 3;
     if (cudaGetLastError() != cudaSuccess) return false;
@@ -347,6 +363,32 @@ int32_t walk_keys(uastar_engine *eng, uint32_t goal_slot, uint64_t cap, std::vec
     return UASTAR_OK;
 }
 
+// Boards goal -> start of a 16-byte-key search, reversed to start -> goal.
+int32_t walk_keys_wide(uastar_engine *eng, uint32_t goal_slot, uint64_t cap, std::vector<Key128> *keys) {
+    cudaError_t e;
+    if ((e = eng->walk.ensure((size_t)cap * 16 + 64)) != cudaSuccess) return fail_cuda(eng, e, "alloc walk");
+    unsigned long long *d_keys = eng->walk.as<unsigned long long>();
+    unsigned long long *d_len = d_keys + 2 * cap;
+    k_walk_wide<<<1, 32, 0, eng->stream>>>(eng->tab.as<Slot>(), goal_slot, d_keys, cap, d_len);
+    eng->launches++;
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(eng, e, "walk launch");
+    unsigned long long len = 0;
+    if ((e = cudaMemcpyAsync(&len, d_len, 8, cudaMemcpyDeviceToHost, eng->stream)) != cudaSuccess)
+        return fail_cuda(eng, e, "walk length");
+    if ((e = cudaStreamSynchronize(eng->stream)) != cudaSuccess) return fail_cuda(eng, e, "walk");
+    if (len > cap) {
+        eng->set_err("solution path longer than the walk buffer");
+        return UASTAR_ARENA_FULL;
+    }
+    keys->resize(len);
+    if (len && (e = cudaMemcpyAsync(keys->data(), d_keys, len * 16, cudaMemcpyDeviceToHost, eng->stream)) !=
+                   cudaSuccess)
+        return fail_cuda(eng, e, "walk keys");
+    if ((e = cudaStreamSynchronize(eng->stream)) != cudaSuccess) return fail_cuda(eng, e, "walk copy");
+    std::reverse(keys->begin(), keys->end());
+    return UASTAR_OK;
+}
+
 int32_t grid_load_impl(uastar_engine *eng, const uint64_t *words, int32_t H, int32_t W) {
     if (!eng) return UASTAR_BAD_INPUT;
     if (!words || H <= 0 || W <= 0 || (uint64_t)H * (uint64_t)W >= (1ull << 32)) {
@@ -498,6 +540,16 @@ int32_t puzzle_solve_n(uastar_engine *eng, const uint8_t *tiles, uastar_puzzle_r
     prob.start = pack_board(N, tiles);
     prob.goal = PuzzleProblem<N>::goal_key();
     return run_plain(eng, prob, N == 3 ? 20 : 22, N == 3 ? 1024 : 16383, po);
+}
+
+// 5x5: 16-byte keys (PuzzleProblem<5>)
+template <>
+int32_t puzzle_solve_n<5>(uastar_engine *eng, const uint8_t *tiles, uastar_puzzle_result *, PlainOut *po) {
+    PuzzleProblem<5> prob;
+    prob.pdb = eng->pdb[5].as<uint8_t>();
+    prob.start = PuzzleProblem<5>::pack(tiles);
+    prob.goal = PuzzleProblem<5>::goal_key();
+    return run_plain(eng, prob, 22, 16383, po);
 }
 
 // Moves (0..3, the reference's DX/DY order) between consecutive packed boards.
@@ -681,8 +733,8 @@ int32_t uastar_puzzle_solve(uastar_engine *eng, int32_t n, const uint8_t *tiles,
     eng->last_ok = false;
     eng->path_cached = false;
     eng->last_kind = UASTAR_KIND_PUZZLE;
-    if ((n != 3 && n != 4) || !tiles || !board_ok(n, tiles)) {
-        eng->set_err("puzzle must be 3x3 or 4x4 with tiles 0..n*n-1 once each");
+    if ((n < 3 || n > 5) || !tiles || !board_ok(n, tiles)) {
+        eng->set_err("puzzle must be 3x3, 4x4 or 5x5 with tiles 0..n*n-1 once each");
         return out->status = UASTAR_BAD_INPUT;
     }
     if (!eng->pdb_ready[n]) {
@@ -695,7 +747,9 @@ int32_t uastar_puzzle_solve(uastar_engine *eng, int32_t n, const uint8_t *tiles,
         return out->status;
     }
     PlainOut po;
-    int32_t rc = n == 3 ? puzzle_solve_n<3>(eng, tiles, out, &po) : puzzle_solve_n<4>(eng, tiles, out, &po);
+    int32_t rc = n == 3   ? puzzle_solve_n<3>(eng, tiles, out, &po)
+                 : n == 4 ? puzzle_solve_n<4>(eng, tiles, out, &po)
+                          : puzzle_solve_n<5>(eng, tiles, out, &po);
     if (rc) return out->status = rc;
     const TeamState &st = po.st;
     out->status = (int32_t)st.status;
@@ -708,19 +762,32 @@ int32_t uastar_puzzle_solve(uastar_engine *eng, int32_t n, const uint8_t *tiles,
     out->table_grows = po.grows;
     if (st.status == ST_OK) {
         out->steps = (int32_t)st.goal_best;
-        std::vector<uint64_t> keys;
-        rc = walk_keys(eng, st.goal_slot, 4096, &keys);
-        if (rc) return out->status = rc;
         eng->path.clear();
-        for (size_t i = 1; i < keys.size(); ++i) {
-            auto blank = [n](uint64_t k) {
+        std::vector<int> blanks;  // blank cell of each board, start -> goal
+        if (n == 5) {
+            std::vector<Key128> keys;
+            rc = walk_keys_wide(eng, st.goal_slot, 4096, &keys);
+            if (rc) return out->status = rc;
+            for (const Key128 &k : keys) {
+                int b = 24;
+                for (int c = 0; c < 24; ++c)
+                    if (PuzzleProblem<5>::field(k, c) == 0) b = c;
+                blanks.push_back(b);
+            }
+        } else {
+            std::vector<uint64_t> keys;
+            rc = walk_keys(eng, st.goal_slot, 4096, &keys);
+            if (rc) return out->status = rc;
+            for (uint64_t k : keys) {
+                int b = -1;
                 for (int c = 0; c < n * n; ++c)
-                    if (((k >> (4 * c)) & 15) == 0) return c;
-                return -1;
-            };
-            const int pb = blank(keys[i - 1]), cb = blank(keys[i]);
-            const int d = cb - pb == n ? 0 : cb - pb == -n ? 1 : cb - pb == 1 ? 2 : 3;
-            eng->path.push_back(d);
+                    if (((k >> (4 * c)) & 15) == 0) b = c;
+                blanks.push_back(b);
+            }
+        }
+        for (size_t i = 1; i < blanks.size(); ++i) {
+            const int d = blanks[i] - blanks[i - 1];
+            eng->path.push_back(d == n ? 0 : d == -n ? 1 : d == 1 ? 2 : 3);
         }
         if ((int64_t)eng->path.size() != out->steps ||
             uastar_validate_puzzle_moves(n, tiles, eng->path.data(), (int64_t)eng->path.size()) != UASTAR_OK) {

@@ -60,8 +60,8 @@ struct uastar_engine {
     int32_t gH = 0, gW = 0;
     bool grid_loaded = false;
     // pattern databases, indexed by board side
-    uastar::DevBuf pdb[5];
-    bool pdb_ready[5] = {false, false, false, false, false};
+    uastar::DevBuf pdb[6];
+    bool pdb_ready[6] = {false, false, false, false, false, false};
 
     // last plain solve
     int last_kind = 0;          // UASTAR_KIND_GRID / UASTAR_KIND_PUZZLE
@@ -69,7 +69,7 @@ struct uastar_engine {
     uint32_t last_goal_slot = 0;
     int32_t lsx = 0, lsy = 0, lex = 0, ley = 0;
     int32_t last_n = 0;
-    uint8_t last_tiles[16] = {0};
+    uint8_t last_tiles[25] = {0};
     bool path_cached = false;
     std::vector<int32_t> path;  // grid: cell ids; puzzle: moves
 

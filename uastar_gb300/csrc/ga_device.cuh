@@ -40,6 +40,43 @@ struct __align__(32) Slot {
 };
 static_assert(sizeof(Slot) == 32, "slot must be one sector");
 
+// Slot access by key width.  Narrow keys (grid cells, boards of up to 16
+// cells in 4-bit fields) use the layout above; wide keys (a 5x5 board: 24
+// cells in 5-bit fields, the 25th implied) read the same 32 bytes as
+// {key lo, key hi, g, aux, prev}: the 16-byte key is claimed with one
+// 16-byte CAS and g is lowered with its own 8-byte CAS.
+struct Key128 {
+    unsigned long long lo, hi;
+};
+struct __align__(32) WideSlot {
+    unsigned long long lo, hi, g;
+    uint32_t aux, prev;
+};
+static_assert(sizeof(WideSlot) == 32, "wide slot must be one sector");
+
+struct NarrowSlots {
+    using Key = uint64_t;
+    static constexpr bool kWide = false;
+    __device__ static uint64_t slot_g(const Slot *s) { return __ldcg(&s->g); }
+    __device__ static uint32_t slot_prev(const Slot *s) { return __ldcg(&s->prev); }
+    __device__ static void set_link(Slot *s, uint32_t prev, uint32_t aux) {
+        s->prev = prev;
+        s->aux = aux;
+    }
+};
+struct WideSlots {
+    using Key = Key128;
+    static constexpr bool kWide = true;
+    __device__ static const WideSlot *w(const Slot *s) { return reinterpret_cast<const WideSlot *>(s); }
+    __device__ static WideSlot *w(Slot *s) { return reinterpret_cast<WideSlot *>(s); }
+    __device__ static uint64_t slot_g(const Slot *s) { return __ldcg(&w(s)->g); }
+    __device__ static uint32_t slot_prev(const Slot *s) { return __ldcg(&w(s)->prev); }
+    __device__ static void set_link(Slot *s, uint32_t prev, uint32_t aux) {
+        w(s)->prev = prev;
+        w(s)->aux = aux;
+    }
+};
+
 // A successor whose g strictly improved its slot this round.
 struct __align__(16) Cand {
     uint32_t slot;
@@ -124,6 +161,9 @@ __host__ __device__ __forceinline__ uint64_t mix64(uint64_t k) {
     k ^= k >> 33;
     return k;
 }
+
+__host__ __device__ __forceinline__ uint64_t key_hash(uint64_t k) { return mix64(k); }
+__host__ __device__ __forceinline__ uint64_t key_hash(const Key128 &k) { return mix64(k.lo ^ mix64(k.hi)); }
 
 enum : int { FIND_FOUND = 0, FIND_INSERTED = 1, FIND_FULL = 2 };
 

@@ -16,30 +16,49 @@ namespace {
 
 // Re-insert the occupied slots of `src` (n slots) into `dst` (mask + 1
 // empty slots).  Keys are unique, so an insert only races other keys for an
-// empty slot; prev is copied as is and rewritten by k_grow_links.
+// empty slot; prev is copied as is and rewritten by k_grow_links.  Wide:
+// 16-byte keys (WideSlot layout), claimed with one 16-byte CAS.
+template <bool Wide>
 __global__ void k_grow_move(const Slot *src, uint64_t n, Slot *dst, uint64_t mask, uint32_t *map) {
     for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
         const uint4 a = __ldcg(reinterpret_cast<const uint4 *>(src + s));
         const unsigned long long key = ((unsigned long long)a.y << 32) | a.x;
         if (key == kEmptyKey) continue;
         const uint4 b = __ldcg(reinterpret_cast<const uint4 *>(src + s) + 1);
-        uint64_t h = mix64(key) & mask;
-        for (uint64_t probe = 0; probe <= mask; ++probe) {
-            if (atomicCAS(&dst[h].key, kEmptyKey, key) == kEmptyKey) break;
-            h = (h + 1) & mask;
+        uint64_t h;
+        if constexpr (Wide) {
+            const Key128 k{key, ((unsigned long long)a.w << 32) | a.z};
+            h = key_hash(k) & mask;
+            for (uint64_t probe = 0; probe <= mask; ++probe) {
+                const KeyG old = cas128(dst + h, KeyG{kEmptyKey, kEmptyKey}, KeyG{k.lo, k.hi});
+                if (old.key == kEmptyKey && old.g == kEmptyKey) break;
+                h = (h + 1) & mask;
+            }
+        } else {
+            h = mix64(key) & mask;
+            for (uint64_t probe = 0; probe <= mask; ++probe) {
+                if (atomicCAS(&dst[h].key, kEmptyKey, key) == kEmptyKey) break;
+                h = (h + 1) & mask;
+            }
         }
         uint4 *d = reinterpret_cast<uint4 *>(dst + h);
-        d[0] = make_uint4(a.x, a.y, a.z, a.w);  // key, g
-        d[1] = b;                               // aux, prev (old index), pad
+        d[0] = make_uint4(a.x, a.y, a.z, a.w);  // key and g (narrow), key (wide)
+        d[1] = b;                               // aux, prev (old index) and pad (narrow); g, aux, prev (wide)
         map[s] = (uint32_t)h;
     }
 }
 
+template <bool Wide>
 __global__ void k_grow_links(const Slot *src, uint64_t n, Slot *dst, const uint32_t *map) {
     for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
         if (__ldcg(&src[s].key) == kEmptyKey) continue;
-        const uint32_t p = __ldcg(&src[s].prev);
-        dst[map[s]].prev = p == kNone ? kNone : map[p];
+        if constexpr (Wide) {
+            const uint32_t p = __ldcg(&WideSlots::w(src + s)->prev);
+            WideSlots::w(dst + map[s])->prev = p == kNone ? kNone : map[p];
+        } else {
+            const uint32_t p = __ldcg(&src[s].prev);
+            dst[map[s]].prev = p == kNone ? kNone : map[p];
+        }
     }
 }
 

@@ -40,7 +40,7 @@ __host__ __device__ __forceinline__ int grid_cost_cmp(uint64_t p, uint64_t q) {
     return d > 0 ? s : -s;
 }
 
-struct GridProblem {
+struct GridProblem : NarrowSlots {
     using Entry = GridEntry;
     static constexpr int kMoves = 8;
 
@@ -186,6 +186,19 @@ template <> struct PuzzlePatterns<4> {
     __host__ __device__ static constexpr uint64_t offset(int p) { return p == 0 ? 0ull : 518918400ull; }
 };
 
+// 5x5: the four 6-tile partitions, in the reference's tracked order (the
+// order fixes the rank; src/puzzle/CPU-solver.hpp:71-102).
+template <> struct PuzzlePatterns<5> {
+    static constexpr int kNum = 4;
+    __host__ __device__ static constexpr int count(int) { return 6; }
+    __host__ __device__ static constexpr int tile(int p, int j) {
+        constexpr int t[4][6] = {{3, 4, 5, 10, 15, 20}, {2, 1, 6, 11, 16, 21}, {7, 8, 9, 12, 17, 22},
+                                 {13, 14, 18, 19, 23, 24}};
+        return t[p][j];
+    }
+    __host__ __device__ static constexpr uint64_t offset(int p) { return (uint64_t)p * 127512000ull; }
+};
+
 template <int N> __host__ __device__ constexpr uint32_t pattern_mult(int p, int j) {
     // prod_{i=j}^{k-1} (N*N - i)
     uint32_t m = 1;
@@ -199,7 +212,7 @@ template <int N> __host__ __device__ constexpr int pattern_of_tile(int t) {
     return -1;
 }
 
-template <int N> struct PuzzleProblem {
+template <int N> struct PuzzleProblem : NarrowSlots {
     using Entry = PuzzleEntry;
     static constexpr int kMoves = 4;
     static constexpr int NN = N * N;
@@ -340,6 +353,169 @@ template <int N> struct PuzzleProblem {
         key = v.x;
         g = v.y;
         aux = __ldcg(&s->aux);
+    }
+};
+
+// ------------------------------------------------------- 24-puzzle ---
+// 5x5 board, 128-bit key: cells 0..11 in `lo` and 12..23 in `hi`, 5 bits
+// each; cell 24 is implied (the tiles 0..24 sum to 300), so every state has
+// one key and bits 60..63 of both words stay zero (the all-ones empty key is
+// never a board).  aux = the four pattern parts, 7 bits each, | (last move +
+// 1) << 28.
+template <> struct PuzzleProblem<5> : WideSlots {
+    using Entry = PuzzleEntry;
+    static constexpr int kMoves = 4;
+    static constexpr int N = 5;
+    static constexpr int NN = 25;
+    static constexpr uint64_t kFieldLow = 0x0084210842108421ull;  // bit 0 of each of 12 fields
+
+    const uint8_t *pdb;  // four concatenated tables
+    Key128 start;
+    Key128 goal;
+
+    __device__ static int cost_cmp(uint64_t a, uint64_t b) { return a < b ? -1 : (a > b ? 1 : 0); }
+
+    __host__ __device__ static uint32_t field(const Key128 &k, int i) {
+        if (i < 12) return (uint32_t)(k.lo >> (5 * i)) & 31u;
+        if (i < 24) return (uint32_t)(k.hi >> (5 * (i - 12))) & 31u;
+        uint32_t sum = 0;
+        for (int c = 0; c < 12; ++c) sum += (uint32_t)(k.lo >> (5 * c)) & 31u;
+        for (int c = 0; c < 12; ++c) sum += (uint32_t)(k.hi >> (5 * c)) & 31u;
+        return 300u - sum;
+    }
+    __host__ __device__ static void set_field(Key128 &k, int i, uint32_t v) {
+        if (i < 12)
+            k.lo = (k.lo & ~(31ull << (5 * i))) | ((uint64_t)v << (5 * i));
+        else if (i < 24)
+            k.hi = (k.hi & ~(31ull << (5 * (i - 12)))) | ((uint64_t)v << (5 * (i - 12)));
+        // cell 24 is implied
+    }
+    __host__ __device__ static Key128 pack(const uint8_t *tiles) {
+        Key128 k{0, 0};
+        for (int i = 0; i < 24; ++i) set_field(k, i, tiles[i]);
+        return k;
+    }
+    __host__ __device__ static Key128 goal_key() {
+        Key128 k{0, 0};
+        for (int i = 0; i < 24; ++i) set_field(k, i, (uint32_t)(i + 1));
+        return k;
+    }
+    // index of the zero field of a 60-bit word of 5-bit fields (12 if none)
+    __device__ __forceinline__ static int zero_field(uint64_t w) {
+        const uint64_t t = w | (w >> 1) | (w >> 2) | (w >> 3) | (w >> 4);
+        const uint64_t z = ~t & kFieldLow;
+        return z ? (__ffsll((long long)z) - 1) / 5 : 12;
+    }
+    __device__ __forceinline__ static int blank(const Key128 &k) {
+        const int a = zero_field(k.lo);
+        if (a < 12) return a;
+        const int b = zero_field(k.hi);
+        return b < 12 ? 12 + b : 24;
+    }
+    // cell of each tile, 5 bits per tile, in a 128-bit word
+    __device__ __forceinline__ static unsigned __int128 inverse(const Key128 &k) {
+        unsigned __int128 inv = 0;
+        uint32_t sum = 0;
+#pragma unroll
+        for (int i = 0; i < 24; ++i) {
+            const uint32_t t = i < 12 ? (uint32_t)(k.lo >> (5 * i)) & 31u : (uint32_t)(k.hi >> (5 * (i - 12))) & 31u;
+            sum += t;
+            inv |= (unsigned __int128)i << (5 * t);
+        }
+        inv |= (unsigned __int128)24 << (5 * (300u - sum));
+        return inv;
+    }
+    template <int P> __device__ __forceinline__ static uint32_t rank(unsigned __int128 inv) {
+        uint32_t used = 0, code = 0;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+            const uint32_t pos = (uint32_t)(inv >> (5 * PuzzlePatterns<5>::tile(P, j))) & 31u;
+            const uint32_t v = pos - __popc(used & ((1u << pos) - 1u));
+            code += v * pattern_mult<5>(P, j + 1);
+            used |= 1u << pos;
+        }
+        return code;
+    }
+    __device__ __forceinline__ uint32_t part(int p, unsigned __int128 inv) const {
+        switch (p) {
+        case 0: return __ldg(pdb + PuzzlePatterns<5>::offset(0) + rank<0>(inv));
+        case 1: return __ldg(pdb + PuzzlePatterns<5>::offset(1) + rank<1>(inv));
+        case 2: return __ldg(pdb + PuzzlePatterns<5>::offset(2) + rank<2>(inv));
+        default: return __ldg(pdb + PuzzlePatterns<5>::offset(3) + rank<3>(inv));
+        }
+    }
+    __device__ static uint32_t hsum(uint32_t aux) {
+        return (aux & 127u) + ((aux >> 7) & 127u) + ((aux >> 14) & 127u) + ((aux >> 21) & 127u);
+    }
+
+    __device__ Key128 start_key() const { return start; }
+    __device__ uint32_t start_aux() const {
+        const unsigned __int128 inv = inverse(start);
+        return part(0, inv) | part(1, inv) << 7 | part(2, inv) << 14 | part(3, inv) << 21;
+    }
+    __device__ bool is_goal(const Key128 &k) const { return k.lo == goal.lo && k.hi == goal.hi; }
+    __device__ __forceinline__ uint64_t f_of(const Key128 &, uint64_t g, uint32_t aux) const { return g + hsum(aux); }
+    // Blank moves 0..3 = DX/DY[0..3]; the move undoing the parent's is skipped.
+    __device__ uint32_t moves(const Key128 &k, uint32_t aux) const {
+        const int b = blank(k), bx = b / N, by = b % N;
+        uint32_t m = 0;
+        if (bx + 1 < N) m |= 1u;
+        if (bx > 0) m |= 2u;
+        if (by + 1 < N) m |= 4u;
+        if (by > 0) m |= 8u;
+        const uint32_t last = aux >> 28;
+        if (last) m &= ~(1u << ((last - 1) ^ 1));
+        return m;
+    }
+    struct Succ {
+        Key128 key;
+        uint64_t g;
+        uint32_t part;   // the moved tile's pattern entry
+        uint32_t which;  // its pattern
+    };
+    __device__ __forceinline__ void succ_begin(const Key128 &key, uint64_t g, uint32_t, int mv, Succ &s) const {
+        const int b = blank(key);
+        const int q = b + (mv == 0 ? N : mv == 1 ? -N : mv == 2 ? 1 : -1);
+        const uint32_t t = field(key, q);
+        s.key = key;
+        set_field(s.key, b, t);
+        set_field(s.key, q, 0);
+        s.g = g + 1;
+        s.which = (uint32_t)pattern_of_tile<5>((int)t);
+        s.part = part((int)s.which, inverse(s.key));
+    }
+    __device__ __forceinline__ void succ_end(const Succ &s, uint32_t aux, int mv, uint32_t &naux,
+                                             uint64_t &nf) const {
+        const uint32_t sh = 7u * s.which;
+        uint32_t a = (aux & 0x0fffffffu & ~(127u << sh)) | (s.part << sh);
+        naux = a | ((uint32_t)(mv + 1) << 28);
+        nf = s.g + hsum(naux);
+    }
+    __device__ __forceinline__ Entry make_entry(uint64_t f, uint64_t g, uint32_t slot) const {
+        Entry e;
+        e.key = ((uint32_t)f << 16) | (0xffffu - (uint32_t)g);
+        e.slot = slot;
+        return e;
+    }
+    __device__ __forceinline__ static uint64_t entry_cost(const Entry &e) { return e.key >> 16; }
+    __device__ __forceinline__ static bool less(const Entry &a, const Entry &b) { return a.key < b.key; }
+    __device__ __forceinline__ static Entry load(const Entry *p) {
+        const uint2 u = __ldcg(reinterpret_cast<const uint2 *>(p));
+        Entry e;
+        e.key = u.x;
+        e.slot = u.y;
+        return e;
+    }
+    __device__ __forceinline__ static void store(Entry *p, const Entry &e) {
+        *reinterpret_cast<uint2 *>(p) = make_uint2(e.key, e.slot);
+    }
+    __device__ __forceinline__ static void load_node(const Slot *s, Key128 &key, uint64_t &g, uint32_t &aux) {
+        const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(s));
+        const ulonglong2 w = __ldcg(reinterpret_cast<const ulonglong2 *>(s) + 1);
+        key.lo = v.x;
+        key.hi = v.y;
+        g = w.x;
+        aux = (uint32_t)w.y;
     }
 };
 

@@ -352,7 +352,9 @@ __device__ __forceinline__ KeyG cas128(Slot *s, KeyG cmp, KeyG val) {
     return atomicCAS(reinterpret_cast<KeyG *>(s), cmp, val);
 }
 
-enum : int { RELAX_NONE = 0, RELAX_IMPROVED = 1, RELAX_INSERTED = 3, RELAX_FULL = 4 };
+// Bit 0: g strictly lowered; bit 1: a new slot was claimed; RELAX_FULL: the
+// probe limit was reached.
+enum : int { RELAX_NONE = 0, RELAX_IMPROVED = 1, RELAX_CLAIMED = 2, RELAX_INSERTED = 3, RELAX_FULL = 4 };
 
 // Find-or-insert `key` and lower its g to `g` in one pass.  The home slot is
 // tried with a single 16-byte CAS that either claims it empty with (key, g)
@@ -415,6 +417,42 @@ __device__ __forceinline__ int relax(Slot *tab, uint64_t mask, uint32_t max_prob
     return RELAX_FULL;
 }
 
+// Wide keys: find-or-claim the 16-byte key with one 16-byte CAS per probed
+// slot, then lower the slot's g with an 8-byte CAS loop.  A claimer whose g
+// another writer of the same key has already undercut reports RELAX_CLAIMED.
+template <class P>
+__device__ __forceinline__ int relax_wide(Slot *tab, uint64_t mask, uint32_t max_probe, const Key128 &key,
+                                          uint64_t g, uint32_t *slot_out) {
+    uint64_t h = key_hash(key) & mask;
+    const KeyG empty{kEmptyKey, kEmptyKey};
+    for (uint32_t probe = 0; probe < max_probe; ++probe) {
+        const KeyG cur = cas128(tab + h, empty, KeyG{key.lo, key.hi});
+        const bool claimed = cur.key == kEmptyKey && cur.g == kEmptyKey;
+        if (claimed || (cur.key == key.lo && cur.g == key.hi)) {
+            *slot_out = (uint32_t)h;
+            unsigned long long *gp = &WideSlots::w(tab + h)->g;
+            unsigned long long old = claimed ? kInfCost : __ldcg(gp);
+            while (P::cost_cmp(g, old) < 0) {
+                const unsigned long long seen = atomicCAS(gp, old, (unsigned long long)g);
+                if (seen == old) return claimed ? RELAX_INSERTED : RELAX_IMPROVED;
+                old = seen;
+            }
+            return claimed ? RELAX_CLAIMED : RELAX_NONE;
+        }
+        h = (h + 1) & mask;
+    }
+    return RELAX_FULL;
+}
+
+template <class P>
+__device__ __forceinline__ int relax_key(Slot *tab, uint64_t mask, uint32_t max_probe, const typename P::Key &key,
+                                         uint64_t g, uint32_t *slot_out) {
+    if constexpr (P::kWide)
+        return relax_wide<P>(tab, mask, max_probe, key, g, slot_out);
+    else
+        return relax<P>(tab, mask, max_probe, key, g, slot_out);
+}
+
 __device__ __forceinline__ Cand load_cand(const Cand *p) {
     const uint4 a = __ldcg(reinterpret_cast<const uint4 *>(p));
     const uint4 b = __ldcg(reinterpret_cast<const uint4 *>(p) + 1);
@@ -429,8 +467,9 @@ __device__ __forceinline__ Cand load_cand(const Cand *p) {
 }
 
 // Shared-memory layout of one CTA of a search team.
-struct PopInfo {
-    unsigned long long key, g;
+template <class Key> struct PopInfo {
+    Key key;
+    unsigned long long g;
     uint32_t aux, slot, mask, excl;  // excl: exclusive prefix of successor counts
 };
 
@@ -449,7 +488,9 @@ template <class P> struct SearchSmem {
     // entries of a heap's insertion buffer: two rounds of pushes
     static constexpr uint32_t kBuf = 2 * P::kMoves;
     // pops, heap tops, brick scratch, insertion buffers, then warp totals
-    static __host__ __device__ size_t tops_offset(uint32_t H) { return (size_t)H * sizeof(PopInfo); }
+    static __host__ __device__ size_t tops_offset(uint32_t H) {
+        return ((size_t)H * sizeof(PopInfo<typename P::Key>) + 15) & ~(size_t)15;
+    }
     static __host__ __device__ size_t scr_offset(uint32_t H, uint32_t L) {
         return (tops_offset(H) + (size_t)H * (1u << L) * sizeof(E) + 127) & ~(size_t)127;
     }
@@ -518,7 +559,8 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
     const uint32_t rthreads = T - rfirst;
     const bool relaxer = tid >= rfirst;
 
-    PopInfo *pop = reinterpret_cast<PopInfo *>(smem);
+    using Key = typename P::Key;
+    PopInfo<Key> *pop = reinterpret_cast<PopInfo<Key> *>(smem);
     E *tops = reinterpret_cast<E *>(smem + SearchSmem<P>::tops_offset(H));
     E *scr = reinterpret_cast<E *>(smem + SearchSmem<P>::scr_offset(H, L));
     uint32_t *scratch = reinterpret_cast<uint32_t *>(smem + SearchSmem<P>::scratch_offset(H, L));
@@ -543,14 +585,13 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
     team.sync();
     if (fresh) {
         if (cta == 0 && tid == 0) {
-            const uint64_t key0 = prob.start_key();
+            const Key key0 = prob.start_key();
             const uint32_t aux0 = prob.start_aux();
             uint32_t s0;
-            if (relax<P>(m.tab, m.mask, m.max_probe, key0, 0, &s0) == RELAX_FULL) {
+            if (relax_key<P>(m.tab, m.mask, m.max_probe, key0, 0, &s0) == RELAX_FULL) {
                 set_error(&st->error, ST_HASH_FULL);
             } else {
-                m.tab[s0].aux = aux0;
-                m.tab[s0].prev = kNone;
+                P::set_link(m.tab + s0, kNone, aux0);
                 uint32_t sz = 0;
                 heap_push<P>(myheap, sz, prob.make_entry(prob.f_of(key0, 0, aux0), 0, s0));
                 m.heap_size[myh] = sz;
@@ -623,7 +664,8 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
             const uint64_t wmin = warp_min_cost<P>(ecost);
             if (lane == 0 && wmin != kInfCost) atomic_min_cost<P>(&st->round_min[r3], wmin);
             if (have) {
-                uint64_t key, g;
+                Key key;
+                uint64_t g;
                 uint32_t aux;
                 P::load_node(m.tab + e.slot, key, g, aux);
                 const uint64_t fcur = prob.f_of(key, g, aux);
@@ -709,19 +751,19 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                         else
                             hi = mid - 1;
                     }
-                    const PopInfo &pi = pop[lo];
+                    const PopInfo<Key> &pi = pop[lo];
                     const int move = (int)__fns(pi.mask, 0, (int)(j - pi.excl) + 1);
                     oslot = pi.slot;
                     typename P::Succ sc;
                     prob.succ_begin(pi.key, pi.g, pi.aux, move, sc);
                     ng = sc.g;
                     ++nS;
-                    const int r = relax<P>(m.tab, m.mask, m.max_probe, sc.key, sc.g, &nslot);
+                    const int r = relax_key<P>(m.tab, m.mask, m.max_probe, sc.key, sc.g, &nslot);
                     prob.succ_end(sc, pi.aux, move, naux, nf);
                     if (r == RELAX_FULL) {
                         set_error(&st->err[r3], ST_HASH_FULL);
                     } else {
-                        inserted = (r == RELAX_INSERTED);
+                        inserted = (r & RELAX_CLAIMED) != 0;
                         improved = (r & RELAX_IMPROVED) != 0;
                     }
                 }
@@ -830,9 +872,8 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
             }
             const Cand c = load_cand(half + (size_t)lo * RR + 1 + (i - roff[lo]));
             E e = prob.make_entry(c.f, c.g, c.slot);
-            if (ldcg_u64(&m.tab[c.slot].g) == c.g) {
-                m.tab[c.slot].prev = c.parent;
-                m.tab[c.slot].aux = c.aux;
+            if (P::slot_g(m.tab + c.slot) == c.g) {
+                P::set_link(m.tab + c.slot, c.parent, c.aux);
             } else {
                 e.slot = kNone;  // lost to a better writer
             }

@@ -79,7 +79,7 @@ int32_t uastar_gen_grid(uint64_t seed, int32_t H, int32_t W, double block_rate, 
 }
 
 int32_t uastar_gen_puzzle(uint64_t seed, int32_t n, int32_t walk_len, uint8_t *tiles) {
-    if (n < 2 || n > 4 || walk_len < 0 || !tiles) return UASTAR_BAD_INPUT;
+    if (n < 2 || n > 5 || walk_len < 0 || !tiles) return UASTAR_BAD_INPUT;
     const int nn = n * n;
     for (int i = 0; i < nn; ++i) tiles[i] = (uint8_t)((i + 1) % nn);
     int bx = n - 1, by = n - 1, last = -1;
@@ -231,9 +231,9 @@ int32_t uastar_validate_grid_path(const uint64_t *words, int32_t H, int32_t W, i
 
 int32_t uastar_validate_puzzle_moves(int32_t n, const uint8_t *tiles, const int32_t *moves,
                                      int64_t len) {
-    if (n < 2 || n > 4 || !tiles || (len > 0 && !moves)) return UASTAR_BAD_INPUT;
+    if (n < 2 || n > 5 || !tiles || (len > 0 && !moves)) return UASTAR_BAD_INPUT;
     const int nn = n * n;
-    uint8_t b[16];
+    uint8_t b[25];
     int seen = 0, bx = -1, by = -1;
     for (int i = 0; i < nn; ++i) {
         b[i] = tiles[i];

@@ -114,6 +114,15 @@ std::vector<PatternDesc> patterns_of(int n) {
         PatternDesc b{4, 7, {7, 8, 10, 11, 12, 14, 15, 0}, 57657600ull, 518918400ull};
         v.push_back(a);
         v.push_back(b);
+    } else if (n == 5) {
+        // src/puzzle/CPU-solver.hpp:71-102, in its tracked order
+        const int t[4][6] = {{3, 4, 5, 10, 15, 20}, {2, 1, 6, 11, 16, 21}, {7, 8, 9, 12, 17, 22},
+                             {13, 14, 18, 19, 23, 24}};
+        for (int p = 0; p < 4; ++p) {
+            PatternDesc d{5, 6, {t[p][0], t[p][1], t[p][2], t[p][3], t[p][4], t[p][5], 0, 0}, 127512000ull,
+                          (uint64_t)p * 127512000ull};
+            v.push_back(d);
+        }
     }
     return v;
 }
@@ -132,6 +141,31 @@ uint64_t goal_rank(const PatternDesc &p) {
         used |= 1u << cell;
     }
     return code;
+}
+
+__global__ void k_pdb_max(const uint8_t *t, uint64_t n, uint32_t *mx) {
+    uint32_t m = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        m = max(m, (uint32_t)t[i]);
+    atomicMax(mx, m);
+}
+
+// Fails unless every entry is <= limit.
+int32_t check_max(uastar_engine *eng, const uint8_t *t, uint64_t n, uint32_t limit) {
+    uastar::DevBuf d;
+    cudaError_t e;
+    if ((e = d.ensure(64)) != cudaSuccess) return fail_cuda(eng, e, "pdb check");
+    cudaMemsetAsync(d.p, 0, 4, eng->stream);
+    k_pdb_max<<<eng->sms * 4, 256, 0, eng->stream>>>(t, n, d.as<uint32_t>());
+    eng->launches++;
+    uint32_t mx = 0;
+    cudaMemcpyAsync(&mx, d.p, 4, cudaMemcpyDeviceToHost, eng->stream);
+    if ((e = cudaStreamSynchronize(eng->stream)) != cudaSuccess) return fail_cuda(eng, e, "pdb check");
+    if (mx > limit) {
+        eng->set_err("pattern database entry above the search's field width");
+        return UASTAR_CUDA_ERROR;
+    }
+    return UASTAR_OK;
 }
 
 template <int N, int P>
@@ -174,7 +208,7 @@ namespace uastar {
 int32_t pdb_build_device(uastar_engine *eng, int n, double *ms) {
     const auto pats = patterns_of(n);
     if (pats.empty()) {
-        eng->set_err("pattern databases exist for n = 3 and n = 4");
+        eng->set_err("pattern databases exist for n = 3, 4 and 5");
         return UASTAR_BAD_INPUT;
     }
     const int64_t bytes = uastar_pdb_bytes(n);
@@ -189,9 +223,16 @@ int32_t pdb_build_device(uastar_engine *eng, int n, double *ms) {
     int32_t rc = UASTAR_OK;
     if (n == 3) {
         rc = build_one<3, 0>(eng, base, pats[0].size, goal_rank(pats[0]));
-    } else {
+    } else if (n == 4) {
         rc = build_one<4, 0>(eng, base + pats[0].offset, pats[0].size, goal_rank(pats[0]));
         if (!rc) rc = build_one<4, 1>(eng, base + pats[1].offset, pats[1].size, goal_rank(pats[1]));
+    } else {
+        rc = build_one<5, 0>(eng, base + pats[0].offset, pats[0].size, goal_rank(pats[0]));
+        if (!rc) rc = build_one<5, 1>(eng, base + pats[1].offset, pats[1].size, goal_rank(pats[1]));
+        if (!rc) rc = build_one<5, 2>(eng, base + pats[2].offset, pats[2].size, goal_rank(pats[2]));
+        if (!rc) rc = build_one<5, 3>(eng, base + pats[3].offset, pats[3].size, goal_rank(pats[3]));
+        // the 5x5 search keeps each part in 7 bits
+        if (!rc) rc = check_max(eng, base, (uint64_t)bytes, 127);
     }
     cudaEventRecord(b, eng->stream);
     cudaEventSynchronize(b);
@@ -211,6 +252,7 @@ extern "C" {
 int64_t uastar_pdb_bytes(int32_t n) {
     if (n == 3) return 362880;
     if (n == 4) return 518918400ll + 57657600ll;
+    if (n == 5) return 4ll * 127512000ll;
     return 0;
 }
 

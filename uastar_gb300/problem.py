@@ -206,8 +206,10 @@ class Pathway(Problem):
 
 
 # ------------------------------------------------------------------ puzzle
+# src/puzzle/CPU-solver.hpp:43-102, in the reference's tracked order (it fixes the rank)
 PARTITIONS = {3: [[1, 2, 3, 4, 5, 6, 7, 8]],
-              4: [[1, 2, 3, 4, 5, 6, 9, 13], [7, 8, 10, 11, 12, 14, 15]]}  # src/puzzle/CPU-solver.hpp:43-70
+              4: [[1, 2, 3, 4, 5, 6, 9, 13], [7, 8, 10, 11, 12, 14, 15]],
+              5: [[3, 4, 5, 10, 15, 20], [2, 1, 6, 11, 16, 21], [7, 8, 9, 12, 17, 22], [13, 14, 18, 19, 23, 24]]}
 
 
 def pdb_cache_names(n: int) -> list[str]:
@@ -251,8 +253,8 @@ class Puzzle(Problem):
         if w is not None and h is not None and int(w) != int(h):
             raise ValueError("Currently we force width must equeal to height.")
         self.n = int(w if w is not None else h)
-        if self.n not in (3, 4):
-            raise ValueError("This engine solves N=3 and N=4 puzzles")
+        if self.n not in (3, 4, 5):
+            raise ValueError("This engine solves N=3, N=4 and N=5 puzzles")
         self.opts = dict(options)
         self.stdin = stdin if stdin is not None else sys.stdin
         self.cpu_solver = cpu_solver
