@@ -361,6 +361,7 @@ def section_mb(eng, args):
     moves, ~7.5e7 states when solved exactly): the returned length next to
     the proven lower bound, for dedup tables capped at 2^20 .. 2^24 slots."""
     from uastar_gb300 import workloads as WL
+    from uastar_gb300.engine import gen_puzzle as E_gen_puzzle
     ensure_pdb(eng)
     tiles = WL.mixed_1024()[127].tiles()
     out = []
@@ -372,6 +373,14 @@ def section_mb(eng, args):
     opt = eng.puzzle_solve(4, tiles)
     for row in out:
         row["optimal_steps"] = opt.steps
+    # a 5x5 board 400 random moves from the goal (beyond exact A* in memory)
+    eng.pdb_build(5)
+    t5 = E_gen_puzzle(77, 5, 400)
+    for log2 in (22, 24):
+        r = eng.puzzle_solve_bounded(5, t5, log2)
+        out.append({"puzzle": "5x5, 400-move walk", "max_table_slots": 1 << log2, "table_mb": (1 << log2) * 32 >> 20,
+                    "status": r["status"], "steps": r["steps"], "lower_bound": r["lower_bound"],
+                    "segments": r["segments"], "expanded": r["expanded"], "solve_ms": round(r["solve_ms"], 1)})
     return out
 
 

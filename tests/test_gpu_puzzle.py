@@ -101,8 +101,10 @@ def test_unsolvable_and_bad_boards(peng):
     assert r.status == L.NO_SOLUTION
     with pytest.raises(EngineError):
         peng.puzzle_solve(4, [1, 1] + list(range(3, 16)) + [0])
+    r = peng.puzzle_solve(5, [2, 1] + list(range(3, 25)) + [0])  # odd permutation, n odd
+    assert r.status == L.NO_SOLUTION
     with pytest.raises(EngineError):
-        peng.puzzle_solve(5, list(range(25)))
+        peng.puzzle_solve(6, list(range(36)))
 
 
 def test_goal_board_is_zero_moves(peng):
@@ -175,3 +177,15 @@ def test_puzzle24_golden(peng):
         assert r.ok and r.steps == row["ref"]["steps"], row
         mv = peng.puzzle_moves()
         assert len(mv) == r.steps and E.validate_puzzle_moves(5, row["tiles"], mv)
+
+
+def test_memory_bounded_24_puzzle(peng):
+    """The mode the reference's README describes for puzzles beyond A*'s
+    memory: a 5x5 board 400 random moves from the goal, table capped at
+    2^23 slots (256 MB) — a valid solution and a proven lower bound under it."""
+    tiles = E.gen_puzzle(77, 5, 400)
+    r = peng.puzzle_solve_bounded(5, tiles, 23)
+    assert r["status"] == L.OK
+    assert 0 < r["lower_bound"] <= r["steps"]
+    mv = peng.puzzle_moves()
+    assert len(mv) == r["steps"] and E.validate_puzzle_moves(5, tiles, mv)

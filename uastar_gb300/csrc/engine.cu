@@ -52,7 +52,8 @@ __global__ void k_best_open(PuzzleProblem<N> prob, SearchMem<PuzzleEntry> m, uin
         const uint32_t h = (uint32_t)(t / topn), i = (uint32_t)(t % topn) + 1;
         if (i > __ldcg(&m.heap_size[h])) continue;
         const PuzzleEntry e = PuzzleProblem<N>::load(m.heaps + (size_t)h * m.stride + i);
-        uint64_t key, g;
+        typename PuzzleProblem<N>::Key key;
+        uint64_t g;
         uint32_t aux;
         PuzzleProblem<N>::load_node(m.tab + e.slot, key, g, aux);
         if (prob.f_of(key, g, aux) != PuzzleProblem<N>::entry_cost(e)) continue;  // stale
@@ -552,16 +553,40 @@ int32_t puzzle_solve_n<5>(uastar_engine *eng, const uint8_t *tiles, uastar_puzzl
     return run_plain(eng, prob, 22, 16383, po);
 }
 
-// Moves (0..3, the reference's DX/DY order) between consecutive packed boards.
-void keys_to_moves(int n, const std::vector<uint64_t> &keys, std::vector<int32_t> *moves) {
-    auto blank = [n](uint64_t k) {
+// Boards (tiles per cell) along the prev chain ending at `slot`, start first.
+template <int N>
+int32_t walk_boards(uastar_engine *eng, uint32_t slot, std::vector<std::vector<uint8_t>> *boards) {
+    boards->clear();
+    if constexpr (N == 5) {
+        std::vector<Key128> keys;
+        if (int32_t rc = walk_keys_wide(eng, slot, 4096, &keys)) return rc;
+        for (const Key128 &k : keys) {
+            std::vector<uint8_t> b(25);
+            for (int c = 0; c < 25; ++c) b[c] = (uint8_t)PuzzleProblem<5>::field(k, c);
+            boards->push_back(b);
+        }
+    } else {
+        std::vector<uint64_t> keys;
+        if (int32_t rc = walk_keys(eng, slot, 4096, &keys)) return rc;
+        for (uint64_t k : keys) {
+            std::vector<uint8_t> b(N * N);
+            for (int c = 0; c < N * N; ++c) b[c] = (uint8_t)((k >> (4 * c)) & 15);
+            boards->push_back(b);
+        }
+    }
+    return UASTAR_OK;
+}
+
+// Moves (0..3, the reference's DX/DY order) between consecutive boards.
+void boards_to_moves(int n, const std::vector<std::vector<uint8_t>> &boards, std::vector<int32_t> *moves) {
+    auto blank = [n](const std::vector<uint8_t> &b) {
         for (int c = 0; c < n * n; ++c)
-            if (((k >> (4 * c)) & 15) == 0) return c;
+            if (b[c] == 0) return c;
         return -1;
     };
-    for (size_t i = 1; i < keys.size(); ++i) {
-        const int pb = blank(keys[i - 1]), cb = blank(keys[i]);
-        moves->push_back(cb - pb == n ? 0 : cb - pb == -n ? 1 : cb - pb == 1 ? 2 : 3);
+    for (size_t i = 1; i < boards.size(); ++i) {
+        const int d = blank(boards[i]) - blank(boards[i - 1]);
+        moves->push_back(d == n ? 0 : d == -n ? 1 : d == 1 ? 2 : 3);
     }
 }
 
@@ -574,13 +599,16 @@ void keys_to_moves(int n, const std::vector<uint64_t> &keys, std::vector<int32_t
 template <int N>
 int32_t puzzle_bounded_n(uastar_engine *eng, const uint8_t *tiles, int max_log2, uastar_bounded_result *out,
                          std::vector<int32_t> *moves) {
-    uint8_t cur[16];
+    uint8_t cur[25];
     std::memcpy(cur, tiles, N * N);
     cudaError_t e;
     for (int seg = 0; seg < 256; ++seg) {
         PuzzleProblem<N> prob;
         prob.pdb = eng->pdb[N].as<uint8_t>();
-        prob.start = pack_board(N, cur);
+        if constexpr (N == 5)
+            prob.start = PuzzleProblem<5>::pack(cur);
+        else
+            prob.start = pack_board(N, cur);
         prob.goal = PuzzleProblem<N>::goal_key();
         PlainOut po;
         int32_t rc = run_plain(eng, prob, std::min(N == 3 ? 20 : 22, max_log2), N == 3 ? 1024 : 16383, &po, max_log2);
@@ -589,11 +617,11 @@ int32_t puzzle_bounded_n(uastar_engine *eng, const uint8_t *tiles, int max_log2,
         out->expanded += (int64_t)po.st.expanded;
         out->generated += (int64_t)po.st.generated;
         out->kernel_ms += po.kernel_ms;
-        std::vector<uint64_t> keys;
+        std::vector<std::vector<uint8_t>> boards;
         if (po.st.status == ST_OK) {
             if (seg == 0) out->lower_bound = (int32_t)po.st.goal_best;
-            if ((rc = walk_keys(eng, po.st.goal_slot, 4096, &keys))) return rc;
-            keys_to_moves(N, keys, moves);
+            if ((rc = walk_boards<N>(eng, po.st.goal_slot, &boards))) return rc;
+            boards_to_moves(N, boards, moves);
             return UASTAR_OK;
         }
         if (po.st.status != ST_RUNNING) return (int32_t)po.st.status;
@@ -613,13 +641,13 @@ int32_t puzzle_bounded_n(uastar_engine *eng, const uint8_t *tiles, int max_log2,
         }
         const uint32_t f = (uint32_t)(best >> 48);  // entry key = f << 16 | (0xffff - g)
         if (seg == 0) out->lower_bound = (int32_t)f;
-        if ((rc = walk_keys(eng, (uint32_t)best, 4096, &keys))) return rc;
-        if (keys.size() < 2) {
+        if ((rc = walk_boards<N>(eng, (uint32_t)best, &boards))) return rc;
+        if (boards.size() < 2) {
             eng->set_err("bounded search: the best open node is the start");
             return UASTAR_HASH_FULL;
         }
-        keys_to_moves(N, keys, moves);
-        for (int c = 0; c < N * N; ++c) cur[c] = (uint8_t)((keys.back() >> (4 * c)) & 15);
+        boards_to_moves(N, boards, moves);
+        std::memcpy(cur, boards.back().data(), N * N);
     }
     eng->set_err("bounded search: segment limit reached");
     return UASTAR_ITER_LIMIT;
@@ -815,8 +843,8 @@ int32_t uastar_puzzle_solve_bounded(uastar_engine *eng, int32_t n, const uint8_t
     eng->last_ok = false;
     eng->path_cached = false;
     eng->last_kind = UASTAR_KIND_PUZZLE;
-    if ((n != 3 && n != 4) || !tiles || !board_ok(n, tiles) || max_log2_slots < 16 || max_log2_slots > 31) {
-        eng->set_err("bounded solve: 3x3 or 4x4 board with tiles 0..n*n-1 once each, 16 <= max_log2_slots <= 31");
+    if (n < 3 || n > 5 || !tiles || !board_ok(n, tiles) || max_log2_slots < 16 || max_log2_slots > 31) {
+        eng->set_err("bounded solve: 3x3, 4x4 or 5x5 board with tiles 0..n*n-1 once each, 16 <= max_log2_slots <= 31");
         return out->status = UASTAR_BAD_INPUT;
     }
     if (!eng->pdb_ready[n]) {
@@ -829,8 +857,9 @@ int32_t uastar_puzzle_solve_bounded(uastar_engine *eng, int32_t n, const uint8_t
         return out->status;
     }
     std::vector<int32_t> moves;
-    int32_t rc = n == 3 ? puzzle_bounded_n<3>(eng, tiles, max_log2_slots, out, &moves)
-                        : puzzle_bounded_n<4>(eng, tiles, max_log2_slots, out, &moves);
+    int32_t rc = n == 3   ? puzzle_bounded_n<3>(eng, tiles, max_log2_slots, out, &moves)
+                 : n == 4 ? puzzle_bounded_n<4>(eng, tiles, max_log2_slots, out, &moves)
+                          : puzzle_bounded_n<5>(eng, tiles, max_log2_slots, out, &moves);
     out->status = rc;
     if (rc == UASTAR_OK) {
         out->steps = (int32_t)moves.size();
