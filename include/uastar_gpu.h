@@ -214,7 +214,7 @@ typedef struct {
     int64_t generated;
     int64_t rounds;
     int32_t attempts;         /* 1 + retries with a larger partition */
-    int32_t reserved;
+    int32_t migrations;       /* serving: moves to a cluster slot with the search state kept */
     double latency_ms;        /* serving: completion - arrival; batch: completion - launch */
     double device_ms;         /* device time of the last attempt's search (CTA team) */
     double start_ms;          /* batch: device start of the last attempt, from its wave's first start */

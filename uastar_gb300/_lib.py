@@ -60,7 +60,7 @@ class InstanceResult(C.Structure):
     _fields_ = [("status", C.c_int32), ("steps", C.c_int32), ("straight", C.c_int64),
                 ("diagonal", C.c_int64), ("cost", C.c_float), ("pad", C.c_float),
                 ("expanded", C.c_int64), ("generated", C.c_int64), ("rounds", C.c_int64),
-                ("attempts", C.c_int32), ("reserved", C.c_int32), ("latency_ms", C.c_double),
+                ("attempts", C.c_int32), ("migrations", C.c_int32), ("latency_ms", C.c_double),
                 ("device_ms", C.c_double), ("start_ms", C.c_double)]
 
 

@@ -293,6 +293,40 @@ __global__ void k_batch_walk(const InstDesc *descs, const InstOut *outs, const u
     lens[t] = walk_chain(tab + descs[i].tab_off, outs[i].goal_slot, keys + key_off[t], key_cap[t]);
 }
 
+// Move a parked single-CTA search's heaps (hs heaps) onto a cluster slot's
+// hd = 8 hs heaps: destination heap j takes every (hd / hs)-th entry of source
+// heap j % hs and pushes it into its (empty) heap, one thread per destination
+// heap, with the heap's saved top in global memory and its brick scratch in
+// shared memory.  The dedup partition and the team state carry over as they
+// are, so the search resumes where it stopped.  Sets *err on overflow.
+template <class P>
+__global__ void __launch_bounds__(128) k_migrate_heaps(const typename P::Entry *src, uint32_t src_stride,
+                                                       const uint32_t *src_size, uint32_t hs,
+                                                       typename P::Entry *dst, uint32_t dst_stride,
+                                                       uint32_t *dst_size, uint32_t hd, uint32_t L, uint32_t hcap,
+                                                       uint32_t *err) {
+    using E = typename P::Entry;
+    __shared__ __align__(16) E scr[128 * 2 * BrickHeap<P>::BE];
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= hd) return;
+    const uint32_t topn = (1u << L) - 1u, sh = j % hs, ratio = hd / hs;
+    const E *sblock = src + (size_t)sh * src_stride;
+    const BrickHeap<P> from{const_cast<E *>(sblock) + top_reserve<P>(L), nullptr, nullptr, L};
+    E *dblock = dst + (size_t)j * dst_stride;
+    const BrickHeap<P> to{dblock + top_reserve<P>(L), dblock, scr + (size_t)threadIdx.x * 2 * BrickHeap<P>::BE, L};
+    const uint32_t n_src = src_size[sh];
+    uint32_t n = 0;
+    for (uint32_t i = 1 + j / hs; i <= n_src; i += ratio) {
+        const E e = i <= topn ? P::load(sblock + i) : P::load(from.g + from.off(i));
+        if (n + 1 > hcap) {
+            atomicExch(err, 1u);
+            break;
+        }
+        heap_push<P>(to, n, e);
+    }
+    dst_size[j] = n;
+}
+
 }  // namespace uastar
 
 namespace {
@@ -1347,14 +1381,81 @@ static void serve_grow(ServeState *S, ServeTier &t, int q) {
     d.grow_at = new_n / 2;
 }
 
+// Move CTA slot q's parked request onto a free cluster slot without
+// restarting it (k_migrate_heaps; the team state is copied, the partition and
+// bitmap stay).  Returns false, changing nothing, when no cluster slot, CTA
+// share or heap space is free.
+static bool serve_migrate(ServeState *S, int q) {
+    ServeTier &small = S->tier[0], &large = S->tier[1];
+    const int q2 = large.free_slot();
+    if (q2 < 0 || small.resident() - 1 + 8 * (large.resident() + 1) > S->capacity) return false;
+    ServeSlot &from = small.slots[q];
+    InstDesc d = small.descs[q];
+    const bool grid = d.kind == UASTAR_KIND_GRID;
+    const uint64_t hd = (uint64_t)large.geo.H * 8;
+    const uint64_t hn = (hd * d.heap_stride * (grid ? 16 : 8) + 127) / 128 * 8;  // 16-byte units
+    uint64_t hoff = 0;
+    if (!S->heap_alloc.alloc(hn, 8, &hoff)) return false;
+    uastar_engine *eng = S->eng;
+    if (small.d_map.ensure(64) != cudaSuccess) {
+        S->heap_alloc.release(hoff, hn);
+        return false;
+    }
+    uint32_t *d_err = small.d_map.as<uint32_t>();
+    cudaMemsetAsync(d_err, 0, 4, small.stream);
+    const uint32_t hs = small.geo.H;
+    const uint32_t *src_size = small.d_hsize.as<uint32_t>() + (size_t)q * hs;
+    uint32_t *dst_size = large.d_hsize.as<uint32_t>() + (size_t)q2 * hd;
+    const unsigned blocks = (unsigned)((hd + 127) / 128);
+    if (grid)
+        k_migrate_heaps<GridProblem><<<blocks, 128, 0, small.stream>>>(
+            reinterpret_cast<const GridEntry *>(S->heaps.as<uint8_t>() + d.heap_off), d.heap_stride, src_size, hs,
+            reinterpret_cast<GridEntry *>(S->heaps.as<uint8_t>() + hoff * 16), d.heap_stride, dst_size, (uint32_t)hd,
+            small.geo.L_grid, d.heap_hcap, d_err);
+    else
+        k_migrate_heaps<PuzzleProblem<4>><<<blocks, 128, 0, small.stream>>>(
+            reinterpret_cast<const PuzzleEntry *>(S->heaps.as<uint8_t>() + d.heap_off), d.heap_stride, src_size, hs,
+            reinterpret_cast<PuzzleEntry *>(S->heaps.as<uint8_t>() + hoff * 16), d.heap_stride, dst_size,
+            (uint32_t)hd, small.geo.L_puzzle, d.heap_hcap, d_err);
+    eng->launches++;
+    cudaMemcpyAsync(large.d_states.as<TeamState>() + q2, small.d_states.as<TeamState>() + q, sizeof(TeamState),
+                    cudaMemcpyDeviceToDevice, small.stream);
+    uint32_t err = 0;
+    cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, small.stream);
+    if (cudaStreamSynchronize(small.stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+        S->loop_error = UASTAR_CUDA_ERROR;
+        return false;
+    }
+    if (err) {  // the per-heap capacity is the same: spread over 8x the heaps this cannot overflow
+        S->heap_alloc.release(hoff, hn);
+        return false;
+    }
+    // the request now lives on cluster slot q2
+    S->heap_alloc.release(from.heap_off, from.heap_n);
+    ServeSlot &to = large.slots[q2];
+    to = std::move(from);
+    to.req.acc.migrations += 1;
+    to.heap_off = hoff;
+    to.heap_n = hn;
+    from = ServeSlot();
+    small.descs[q].kind = 0;
+    d.heap_off = hoff * 16;
+    d.key_off = (uint64_t)q2 * large.kcap;
+    d.key_cap = large.kcap;
+    d.fresh = 0;
+    large.descs[q2] = d;
+    return true;
+}
+
 // Retire tier t's finished quantum: completed requests report; one that
 // overflows its CTA slot restarts on a cluster slot with more space, one that
-// overflows a cluster slot retries there with more.  While the GPU has idle
-// CTAs and nothing is waiting (`spare`), a request that keeps its CTA's heaps
-// saturated (a wide frontier, which more heaps would cover in fewer rounds)
-// also moves to a cluster slot, trading throughput for its latency; under
-// load every request stays on one CTA, the most work per CTA.  A grid with a
-// thin frontier never moves: its rounds are bounded by its path length,
+// overflows a cluster slot retries there with more.  A request that keeps its
+// CTA's heaps saturated (a wide frontier, which more heaps cover in fewer
+// rounds) moves to a cluster slot with its search state (serve_migrate) when
+// the GPU has spare CTAs and nothing waits (`spare`: latency), or once it has
+// taken 4M expansions (a request that large would otherwise be the stream's
+// tail); other requests stay on one CTA, the most work per CTA.  A grid with
+// a thin frontier never moves: its rounds are bounded by its path length,
 // which a cluster would not shorten.
 static void serve_retire(ServeState *S, ServeTier &t, std::deque<ServeReq> &to_large, bool spare) {
     ServeTier &large = S->tier[1];
@@ -1370,18 +1471,15 @@ static void serve_retire(ServeState *S, ServeTier &t, std::deque<ServeReq> &to_l
         const InstOut &o = t.outs[q];
         ServeReq &r = sl.req;
         if (o.status == ST_RUNNING) {
-            const bool saturated = o.rounds >= 1024 && (double)o.expanded >= 0.5 * t.geo.H * (double)o.rounds;
-            if (!t.large && saturated && spare && large.nslots > 0 && to_large.empty()) {
-                r.acc.expanded += (int64_t)o.expanded;
-                r.acc.generated += (int64_t)o.generated;
-                r.acc.rounds += (int64_t)o.rounds;
-                r.mult = std::max<uint64_t>(r.mult * 4, 4);
-                serve_release(S, sl);
-                to_large.push_back(std::move(r));
-                sl = ServeSlot();
-                t.descs[q].kind = 0;
-            } else if (t.descs[q].grow_at && o.inserted > t.descs[q].grow_at) {
+            if (t.descs[q].grow_at && o.inserted > t.descs[q].grow_at) {
                 serve_grow(S, t, q);
+                if (S->loop_error) return;
+            }
+            // a wide frontier that has already taken 4M expansions (or any, when
+            // the GPU has spare CTAs) moves to a cluster slot, search state and all
+            const bool saturated = o.rounds >= 1024 && (double)o.expanded >= 0.5 * t.geo.H * (double)o.rounds;
+            if (!t.large && saturated && large.nslots > 0 && to_large.empty() && (spare || o.expanded >= 4000000ull)) {
+                if (serve_migrate(S, q)) continue;
                 if (S->loop_error) return;
             }
             continue;

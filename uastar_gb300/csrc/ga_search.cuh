@@ -86,7 +86,9 @@ struct GridTeam {
 // A thread-block cluster as one team: CTA rank within the cluster, hardware
 // cluster barrier (barrier.cluster arrive.release / wait.acquire; all CTAs of
 // a cluster are co-scheduled, so the barrier needs no time bound), team
-// state in global memory read through L2.
+// state in global memory read through L2.  The barrier's release/acquire at
+// cluster scope orders every memory access of the cluster's threads, global
+// ones included, so no separate fence is needed.
 struct ClusterTeam {
     TeamState *st;  // global memory
     __device__ uint32_t cta() const {
@@ -100,7 +102,6 @@ struct ClusterTeam {
         return r;
     }
     __device__ void sync() {
-        __threadfence();
         asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
     }
     __device__ uint64_t rd64(const unsigned long long *p) const { return ldcg_u64(p); }
