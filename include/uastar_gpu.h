@@ -227,6 +227,8 @@ typedef struct {
     double load_factor;           /* target dedup-partition load (0 -> autotuned) */
     int32_t ctas;                 /* persistent CTAs (0 -> all SMs x occupancy) */
     int32_t use_graph;            /* launch through a captured CUDA graph (default 1) */
+    int32_t tier1_rounds;         /* round budget of a single-CTA team (0 -> 2048) */
+    int32_t tier2_puzzle_rounds;  /* round budget of a puzzle on a cluster team (0 -> 16384) */
 } uastar_batch_config;
 
 typedef struct {

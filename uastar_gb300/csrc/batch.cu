@@ -381,7 +381,7 @@ uint64_t est_nodes(const uastar_instance &in) {
     if (in.est_nodes > 0) return (uint64_t)in.est_nodes;
     // Grids: an eighth of the cells (random grids searched corner to corner
     // touch a few percent to ~20 %).  15-puzzles: 2^19 states, what a single
-    // CTA team inserts in its 4096-round budget (64 heaps, ~2 new states per
+    // CTA team inserts in a 4096-round budget (64 heaps, ~2 new states per
     // expansion), so that a puzzle leaves that tier by running out of rounds
     // rather than out of space.  An instance that fills its partition is
     // re-run in the next wave with 16x the space.
@@ -831,7 +831,8 @@ int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int
     }
     if (!tier1.empty()) {
         std::vector<int> m(tier1.size(), 1);
-        rc = run_wave(eng, insts, tier1, g, m, use_graph, 4096, 0, results, stats, &retry);
+        const uint64_t b1 = cfg && cfg->tier1_rounds > 0 ? (uint64_t)cfg->tier1_rounds : 2048;
+        rc = run_wave(eng, insts, tier1, g, m, use_graph, b1, 0, results, stats, &retry);
         if (rc) return rc;
         // running out of rounds proves an instance large just as an overflow does
         for (int i : retry) {
@@ -854,7 +855,8 @@ int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int
         // off with the whole GPU than holding a cluster for the batch's tail.
         // Grids do not: their rounds are bounded by the path length, which
         // costs a cluster no more rounds than the whole GPU.
-        rc = run_wave(eng, insts, tier2, gc, m, use_graph, ~0ull, 8192, results, stats, &retry);
+        const uint64_t b2 = cfg && cfg->tier2_puzzle_rounds > 0 ? (uint64_t)cfg->tier2_puzzle_rounds : 16384;
+        rc = run_wave(eng, insts, tier2, gc, m, use_graph, ~0ull, b2, results, stats, &retry);
         if (rc) return rc;
         todo = retry;
     }

@@ -501,8 +501,9 @@ template <class P> struct SearchSmem {
     static __host__ __device__ size_t scratch_offset(uint32_t H, uint32_t L) {
         return buf_offset(H, L) + (size_t)H * kBuf * sizeof(E);
     }
-    // warp totals of the block scans, then this CTA's round counters
-    static constexpr uint32_t kScratchWords = 40;
+    // warp totals of the block scans, this CTA's round counters, then the
+    // owner warps' minimum popped f (16 x 8 bytes)
+    static constexpr uint32_t kScratchWords = 72;
     static __host__ __device__ size_t bytes(uint32_t H, uint32_t L) {
         return scratch_offset(H, L) + 4 * kScratchWords;
     }
@@ -594,7 +595,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
             } else {
                 P::set_link(m.tab + s0, kNone, aux0);
                 uint32_t sz = 0;
-                heap_push<P>(myheap, sz, prob.make_entry(prob.f_of(key0, 0, aux0), 0, s0));
+                heap_push<P>(myheap, sz, prob.make_entry(prob.f_of(key0, 0, aux0), 0, s0, aux0));
                 m.heap_size[myh] = sz;
                 st->inserted = 1;
             }
@@ -621,6 +622,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
     const uint64_t RR = cand_region_records<P>(H);
     uint32_t *const s_cnt = scratch + 36;  // this CTA's candidates this round
     uint32_t *const s_ins = scratch + 37;  // dedup slots it claimed this round
+    unsigned long long *const wmins = reinterpret_cast<unsigned long long *>(scratch + 40);  // per owner warp
     // Push-phase staging: one entry per candidate of this CTA's share (at most
     // H * kMoves), then the C + 1 region offsets of the round's candidates
     // (the host keeps C < 32 H); it reuses the sift-down scratch, idle then.
@@ -663,12 +665,16 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
             }
             const uint64_t ecost = have ? P::entry_cost(e) : kInfCost;
             const uint64_t wmin = warp_min_cost<P>(ecost);
-            if (lane == 0 && wmin != kInfCost) atomic_min_cost<P>(&st->round_min[r3], wmin);
+            if (lane == 0) wmins[tid >> 5] = wmin;  // the CTA's minimum goes out once, below
             if (have) {
                 Key key;
                 uint64_t g;
                 uint32_t aux;
                 P::load_node(m.tab + e.slot, key, g, aux);
+                // where the entry names its node (grids), the neighbourhood
+                // reads start now, beside the node record's
+                uint32_t mv_pre = 0;
+                if constexpr (P::kEntryKey) mv_pre = prob.moves(P::entry_key(e), 0);
                 const uint64_t fcur = prob.f_of(key, g, aux);
                 if (fcur != ecost) {
                     // stale: the node was improved after this entry was pushed
@@ -677,7 +683,10 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                     st->goal_slot = e.slot;  // every goal pop names the same slot
                 } else {
                     ++nE;
-                    mv = prob.moves(key, aux);
+                    if constexpr (P::kEntryKey)
+                        mv = mv_pre;
+                    else
+                        mv = prob.moves(key, aux);
                     pop[tid].key = key;
                     pop[tid].g = g;
                     pop[tid].aux = aux;
@@ -702,12 +711,15 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         __syncthreads();
         if (tid == 0) {
             uint32_t acc = 0;
+            uint64_t cmin = kInfCost;
             for (uint32_t w = 0; w < owner_warps; ++w) {
                 const uint32_t t = scratch[2 + w];
                 scratch[2 + w] = acc;
                 acc += t;
+                if (P::cost_cmp(wmins[w], cmin) < 0) cmin = wmins[w];
             }
             scratch[0] = acc;
+            if (cmin != kInfCost) atomic_min_cost<P>(&st->round_min[r3], cmin);
         }
         __syncthreads();
         if (owner) pop[tid].excl += scratch[2 + (tid >> 5)];
@@ -872,7 +884,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                     hi = mid - 1;
             }
             const Cand c = load_cand(half + (size_t)lo * RR + 1 + (i - roff[lo]));
-            E e = prob.make_entry(c.f, c.g, c.slot);
+            E e = prob.make_entry(c.f, c.g, c.slot, c.aux);
             if (P::slot_g(m.tab + c.slot) == c.g) {
                 P::set_link(m.tab + c.slot, c.parent, c.aux);
             } else {
