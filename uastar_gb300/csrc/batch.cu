@@ -92,12 +92,15 @@ struct BatchArgs {
 // returns their number, or cap + 1 if the chain is longer than cap.  One
 // thread: a pointer chase.
 __device__ unsigned long long walk_chain(const Slot *part, uint32_t goal_slot, unsigned long long *out,
-                                         uint64_t cap) {
+                                         uint64_t cap, bool prev_in_key) {
     uint32_t s = goal_slot;
     uint64_t n = 0;
     while (s != kNone && n < cap) {
-        out[n++] = __ldcg(&part[s].key);
-        s = __ldcg(&part[s].prev);
+        uint64_t key;
+        uint32_t prev;
+        slot_key_prev(part + s, prev_in_key, key, prev);
+        out[n++] = key;
+        s = prev;
     }
     return s != kNone ? cap + 1 : n;
 }
@@ -207,7 +210,9 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
             if (o.status == ST_RUNNING && st.error) o.status = st.error;
             // the path is read out now (a batch region is reused by the
             // team's next instance)
-            if (o.status == ST_OK) o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap);
+            if (o.status == ST_OK)
+                o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap,
+                                        d.kind == UASTAR_KIND_GRID && GridProblem::kPrevInKey);
             a.outs[i] = o;
             if (a.serving) a.states[i] = st;
         }
@@ -276,7 +281,9 @@ __global__ void __launch_bounds__(512, 1) k_batch_cluster(BatchArgs a) {
             o.t_end = globaltimer_ns();
             const uint32_t pend = ldcg_u32(&st->error);
             if (o.status == ST_RUNNING && pend) o.status = pend;
-            if (o.status == ST_OK) o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap);
+            if (o.status == ST_OK)
+                o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap,
+                                        d.kind == UASTAR_KIND_GRID && GridProblem::kPrevInKey);
             a.outs[i] = o;
         }
         team.sync();
@@ -290,7 +297,8 @@ __global__ void k_batch_walk(const InstDesc *descs, const InstOut *outs, const u
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nwhich) return;
     const uint32_t i = which[t];
-    lens[t] = walk_chain(tab + descs[i].tab_off, outs[i].goal_slot, keys + key_off[t], key_cap[t]);
+    lens[t] = walk_chain(tab + descs[i].tab_off, outs[i].goal_slot, keys + key_off[t], key_cap[t],
+                         descs[i].kind == UASTAR_KIND_GRID && GridProblem::kPrevInKey);
 }
 
 // Move a parked single-CTA search's heaps (hs heaps) onto a cluster slot's
@@ -1359,8 +1367,13 @@ static void serve_grow(ServeState *S, ServeTier &t, int q) {
     uint32_t *hsize = t.d_hsize.as<uint32_t>() + (size_t)q * k;
     TeamState *st = t.d_states.as<TeamState>() + q;
     fill_ff_async(eng, dst, new_n * sizeof(Slot), t.stream);
-    k_grow_move<false><<<blocks, 256, 0, t.stream>>>(src, old_n, dst, new_n - 1, map);
-    k_grow_links<false><<<blocks, 256, 0, t.stream>>>(src, old_n, dst, map);
+    if (d.kind == UASTAR_KIND_GRID) {
+        k_grow_move<false, GridProblem::kPrevInKey><<<blocks, 256, 0, t.stream>>>(src, old_n, dst, new_n - 1, map);
+        k_grow_links<false, GridProblem::kPrevInKey><<<blocks, 256, 0, t.stream>>>(src, old_n, dst, map);
+    } else {
+        k_grow_move<false, false><<<blocks, 256, 0, t.stream>>>(src, old_n, dst, new_n - 1, map);
+        k_grow_links<false, false><<<blocks, 256, 0, t.stream>>>(src, old_n, dst, map);
+    }
     if (d.kind == UASTAR_KIND_GRID)
         k_grow_heaps<GridProblem><<<blocks, 256, 0, t.stream>>>(
             reinterpret_cast<GridEntry *>(S->heaps.as<uint8_t>() + d.heap_off), d.heap_stride, t.geo.L_grid, hsize,

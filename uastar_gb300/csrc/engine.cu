@@ -64,13 +64,16 @@ __global__ void k_best_open(PuzzleProblem<N> prob, SearchMem<PuzzleEntry> m, uin
 // Walk the prev chain from the goal slot (one thread: a pointer chase).
 // Writes keys goal -> start; *len = count, or cap + 1 when truncated.
 __global__ void k_walk(const Slot *tab, uint32_t goal_slot, unsigned long long *keys,
-                       uint64_t cap, unsigned long long *len) {
+                       uint64_t cap, unsigned long long *len, bool prev_in_key) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     uint32_t s = goal_slot;
     uint64_t n = 0;
     while (s != kNone && n < cap) {
-        keys[n++] = __ldcg(&tab[s].key);
-        s = __ldcg(&tab[s].prev);
+        uint64_t key;
+        uint32_t prev;
+        slot_key_prev(tab + s, prev_in_key, key, prev);
+        keys[n++] = key;
+        s = prev;
     }
     *len = (s != kNone) ? cap + 1 : n;
 }
@@ -187,8 +190,8 @@ bool grow_table(uastar_engine *eng, SearchMem<typename P::Entry> &m, uint32_t k,
     const int blocks = std::max(1, eng->sms * 8);
     Slot *src = m.tab, *dst = eng->tab_next.as<Slot>();
     uint32_t *map = eng->grow_map.as<uint32_t>();
-    k_grow_move<P::kWide><<<blocks, 256, 0, eng->stream>>>(src, old_n, dst, new_n - 1, map);
-    k_grow_links<P::kWide><<<blocks, 256, 0, eng->stream>>>(src, old_n, dst, map);
+    k_grow_move<P::kWide, P::kPrevInKey><<<blocks, 256, 0, eng->stream>>>(src, old_n, dst, new_n - 1, map);
+    k_grow_links<P::kWide, P::kPrevInKey><<<blocks, 256, 0, eng->stream>>>(src, old_n, dst, map);
     k_grow_heaps<P><<<blocks, 256, 0, eng->stream>>>(m.heaps, m.stride, m.L, m.heap_size, k, map, st);
     eng->launches += 3;
     if (cudaGetLastError() != cudaSuccess) return false;
@@ -338,13 +341,14 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
     return UASTAR_OK;
 }
 
-int32_t walk_keys(uastar_engine *eng, uint32_t goal_slot, uint64_t cap, std::vector<uint64_t> *keys) {
+int32_t walk_keys(uastar_engine *eng, uint32_t goal_slot, uint64_t cap, std::vector<uint64_t> *keys,
+                  bool prev_in_key) {
     cudaError_t e;
     const size_t need = (size_t)cap * 8 + 64;
     if ((e = eng->walk.ensure(need)) != cudaSuccess) return fail_cuda(eng, e, "alloc walk");
     unsigned long long *d_keys = eng->walk.as<unsigned long long>();
     unsigned long long *d_len = d_keys + cap;
-    k_walk<<<1, 32, 0, eng->stream>>>(eng->tab.as<Slot>(), goal_slot, d_keys, cap, d_len);
+    k_walk<<<1, 32, 0, eng->stream>>>(eng->tab.as<Slot>(), goal_slot, d_keys, cap, d_len, prev_in_key);
     eng->launches++;
     if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(eng, e, "walk launch");
     unsigned long long len = 0;
@@ -462,7 +466,7 @@ int32_t grid_solve_impl(uastar_engine *eng, const uint64_t *host_words, int32_t 
         // Path: walk prev pointers on the device, re-validate on the host.
         std::vector<uint64_t> keys;
         const uint64_t cap = std::min<uint64_t>(cells + 1, 1ull << 26);
-        rc = walk_keys(eng, st.goal_slot, cap, &keys);
+        rc = walk_keys(eng, st.goal_slot, cap, &keys, GridProblem::kPrevInKey);
         if (rc) return out->status = rc;
         eng->path.assign(keys.size(), 0);
         for (size_t i = 0; i < keys.size(); ++i) eng->path[i] = (int32_t)keys[i];
@@ -567,7 +571,7 @@ int32_t walk_boards(uastar_engine *eng, uint32_t slot, std::vector<std::vector<u
         }
     } else {
         std::vector<uint64_t> keys;
-        if (int32_t rc = walk_keys(eng, slot, 4096, &keys)) return rc;
+        if (int32_t rc = walk_keys(eng, slot, 4096, &keys, false)) return rc;
         for (uint64_t k : keys) {
             std::vector<uint8_t> b(N * N);
             for (int c = 0; c < N * N; ++c) b[c] = (uint8_t)((k >> (4 * c)) & 15);
@@ -804,7 +808,7 @@ int32_t uastar_puzzle_solve(uastar_engine *eng, int32_t n, const uint8_t *tiles,
             }
         } else {
             std::vector<uint64_t> keys;
-            rc = walk_keys(eng, st.goal_slot, 4096, &keys);
+            rc = walk_keys(eng, st.goal_slot, 4096, &keys, false);
             if (rc) return out->status = rc;
             for (uint64_t k : keys) {
                 int b = -1;

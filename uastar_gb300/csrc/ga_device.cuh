@@ -57,6 +57,7 @@ static_assert(sizeof(WideSlot) == 32, "wide slot must be one sector");
 struct NarrowSlots {
     using Key = uint64_t;
     static constexpr bool kWide = false;
+    static constexpr bool kPrevInKey = false;  // see GridProblem
     __device__ static uint64_t slot_g(const Slot *s) { return __ldcg(&s->g); }
     __device__ static uint32_t slot_prev(const Slot *s) { return __ldcg(&s->prev); }
     __device__ static void set_link(Slot *s, uint32_t prev, uint32_t aux) {
@@ -67,6 +68,7 @@ struct NarrowSlots {
 struct WideSlots {
     using Key = Key128;
     static constexpr bool kWide = true;
+    static constexpr bool kPrevInKey = false;
     __device__ static const WideSlot *w(const Slot *s) { return reinterpret_cast<const WideSlot *>(s); }
     __device__ static WideSlot *w(Slot *s) { return reinterpret_cast<WideSlot *>(s); }
     __device__ static uint64_t slot_g(const Slot *s) { return __ldcg(&w(s)->g); }
@@ -76,6 +78,19 @@ struct WideSlots {
         w(s)->aux = aux;
     }
 };
+
+// Key and parent link of a narrow slot; with the link in the key word
+// (grids) the word is cell | prev << 32.  For the path walkers.
+__device__ __forceinline__ void slot_key_prev(const Slot *s, bool prev_in_key, uint64_t &key, uint32_t &prev) {
+    const uint64_t w = __ldcg(&s->key);
+    if (prev_in_key) {
+        key = w & 0xffffffffull;
+        prev = (uint32_t)(w >> 32);
+    } else {
+        key = w;
+        prev = __ldcg(&s->prev);
+    }
+}
 
 // A successor whose g strictly improved its slot this round.
 struct __align__(16) Cand {

@@ -17,8 +17,9 @@ namespace {
 // Re-insert the occupied slots of `src` (n slots) into `dst` (mask + 1
 // empty slots).  Keys are unique, so an insert only races other keys for an
 // empty slot; prev is copied as is and rewritten by k_grow_links.  Wide:
-// 16-byte keys (WideSlot layout), claimed with one 16-byte CAS.
-template <bool Wide>
+// 16-byte keys (WideSlot layout), claimed with one 16-byte CAS.  PrevInKey:
+// the key word is cell | prev << 32 (grids), hashed on the cell.
+template <bool Wide, bool PrevInKey>
 __global__ void k_grow_move(const Slot *src, uint64_t n, Slot *dst, uint64_t mask, uint32_t *map) {
     for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
         const uint4 a = __ldcg(reinterpret_cast<const uint4 *>(src + s));
@@ -35,7 +36,7 @@ __global__ void k_grow_move(const Slot *src, uint64_t n, Slot *dst, uint64_t mas
                 h = (h + 1) & mask;
             }
         } else {
-            h = mix64(key) & mask;
+            h = mix64(PrevInKey ? key & 0xffffffffull : key) & mask;
             for (uint64_t probe = 0; probe <= mask; ++probe) {
                 if (atomicCAS(&dst[h].key, kEmptyKey, key) == kEmptyKey) break;
                 h = (h + 1) & mask;
@@ -48,11 +49,15 @@ __global__ void k_grow_move(const Slot *src, uint64_t n, Slot *dst, uint64_t mas
     }
 }
 
-template <bool Wide>
+template <bool Wide, bool PrevInKey>
 __global__ void k_grow_links(const Slot *src, uint64_t n, Slot *dst, const uint32_t *map) {
     for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
-        if (__ldcg(&src[s].key) == kEmptyKey) continue;
-        if constexpr (Wide) {
+        const uint64_t w = __ldcg(&src[s].key);
+        if (w == kEmptyKey) continue;
+        if constexpr (PrevInKey) {
+            const uint32_t p = (uint32_t)(w >> 32);
+            dst[map[s]].key = (w & 0xffffffffull) | (uint64_t)(p == kNone ? kNone : map[p]) << 32;
+        } else if constexpr (Wide) {
             const uint32_t p = __ldcg(&WideSlots::w(src + s)->prev);
             WideSlots::w(dst + map[s])->prev = p == kNone ? kNone : map[p];
         } else {

@@ -44,6 +44,11 @@ __host__ __device__ __forceinline__ int grid_cost_cmp(uint64_t p, uint64_t q) {
 struct GridProblem : NarrowSlots {
     using Entry = GridEntry;
     static constexpr int kMoves = 8;
+    // Slot key word = cell | prev << 32 (cells are < 2^32 - 1): the relax CAS
+    // sets g and the parent link together, so no push-phase winner check.
+    static constexpr bool kPrevInKey = true;
+    __device__ static uint32_t slot_prev(const Slot *s) { return (uint32_t)(__ldcg(&s->key) >> 32); }
+    __device__ static void set_link(Slot *, uint32_t, uint32_t) {}  // the link lives in the key word
 
     const uint32_t *bm;  // bitmap as 32-bit words (same bytes as the uint64 words)
     int32_t H, W;
@@ -156,9 +161,9 @@ struct GridProblem : NarrowSlots {
     __device__ __forceinline__ static void load_node(const Slot *s, uint64_t &key, uint64_t &g,
                                                      uint32_t &aux) {
         const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(s));
-        key = v.x;
+        key = v.x & 0xffffffffull;
         g = v.y;
-        aux = 0;
+        aux = (uint32_t)key;
     }
 };
 

@@ -363,13 +363,26 @@ enum : int { RELAX_NONE = 0, RELAX_IMPROVED = 1, RELAX_CLAIMED = 2, RELAX_INSERT
 // that is empty or holds the key.  Returns RELAX_INSERTED (new slot, g set),
 // RELAX_IMPROVED (existing slot, g strictly lowered), RELAX_NONE (existing
 // slot, g not better) or RELAX_FULL (probe limit).
+//
+// Where the problem keeps the parent link in the key word (P::kPrevInKey:
+// grid cells are 32 bits), the word is cell | prev << 32 and the CAS sets g
+// and prev together, so the slot's link always belongs to its g: the push
+// phase then needs no winner check.  Keys compare on the cell half.
+template <class P> __device__ __forceinline__ bool key_match(uint64_t word, uint64_t key) {
+    if constexpr (P::kPrevInKey)
+        return (word & 0xffffffffull) == key && word != kEmptyKey;
+    else
+        return word == key;
+}
+
 template <class P>
-__device__ __forceinline__ int relax_at(Slot *tab, uint64_t h, KeyG cur, uint64_t key, uint64_t g,
+__device__ __forceinline__ int relax_at(Slot *tab, uint64_t h, KeyG cur, uint64_t word, uint64_t g,
                                         uint32_t *slot_out) {
-    // cur.key == key: lower g; the key half never changes once set
+    // the slot holds the key: lower g (and, with the link in the key word,
+    // set the link with it)
     *slot_out = (uint32_t)h;
     while (P::cost_cmp(g, cur.g) < 0) {
-        const KeyG old = cas128(tab + h, cur, KeyG{key, g});
+        const KeyG old = cas128(tab + h, cur, KeyG{P::kPrevInKey ? word : cur.key, g});
         if (old.key == cur.key && old.g == cur.g) return RELAX_IMPROVED;
         cur = old;
     }
@@ -378,18 +391,19 @@ __device__ __forceinline__ int relax_at(Slot *tab, uint64_t h, KeyG cur, uint64_
 
 template <class P>
 __device__ __forceinline__ int relax(Slot *tab, uint64_t mask, uint32_t max_probe, uint64_t key, uint64_t g,
-                                     uint32_t *slot_out) {
+                                     uint32_t prev, uint32_t *slot_out) {
     // Linear probing.  The home slot is tried with one 16-byte CAS; past it
     // the probe reads the rest of the home slot's 128-byte line (4 slots) and
     // then whole lines, one dependent load per line.
+    const uint64_t word = P::kPrevInKey ? (key | (uint64_t)prev << 32) : key;
     uint64_t h = mix64(key) & mask;
     const KeyG empty{kEmptyKey, kInfCost};
-    KeyG cur = cas128(tab + h, empty, KeyG{key, g});
+    KeyG cur = cas128(tab + h, empty, KeyG{word, g});
     if (cur.key == kEmptyKey) {
         *slot_out = (uint32_t)h;
         return RELAX_INSERTED;
     }
-    if (cur.key == key) return relax_at<P>(tab, h, cur, key, g, slot_out);
+    if (key_match<P>(cur.key, key)) return relax_at<P>(tab, h, cur, word, g, slot_out);
     uint32_t probed = 1;
     h = (h + 1) & mask;
     while (probed < max_probe) {
@@ -401,14 +415,14 @@ __device__ __forceinline__ int relax(Slot *tab, uint64_t mask, uint32_t max_prob
             if (q < n) v[q] = __ldcg(reinterpret_cast<const ulonglong2 *>(tab + h + q));
         for (uint32_t q = 0; q < n; ++q) {
             const uint64_t hq = h + q;
-            if (v[q].x == key) return relax_at<P>(tab, hq, KeyG{v[q].x, v[q].y}, key, g, slot_out);
+            if (key_match<P>(v[q].x, key)) return relax_at<P>(tab, hq, KeyG{v[q].x, v[q].y}, word, g, slot_out);
             if (v[q].x == kEmptyKey) {
-                cur = cas128(tab + hq, empty, KeyG{key, g});
+                cur = cas128(tab + hq, empty, KeyG{word, g});
                 if (cur.key == kEmptyKey) {
                     *slot_out = (uint32_t)hq;
                     return RELAX_INSERTED;
                 }
-                if (cur.key == key) return relax_at<P>(tab, hq, cur, key, g, slot_out);
+                if (key_match<P>(cur.key, key)) return relax_at<P>(tab, hq, cur, word, g, slot_out);
                 // another key took it: keep probing
             }
         }
@@ -447,11 +461,11 @@ __device__ __forceinline__ int relax_wide(Slot *tab, uint64_t mask, uint32_t max
 
 template <class P>
 __device__ __forceinline__ int relax_key(Slot *tab, uint64_t mask, uint32_t max_probe, const typename P::Key &key,
-                                         uint64_t g, uint32_t *slot_out) {
+                                         uint64_t g, uint32_t prev, uint32_t *slot_out) {
     if constexpr (P::kWide)
         return relax_wide<P>(tab, mask, max_probe, key, g, slot_out);
     else
-        return relax<P>(tab, mask, max_probe, key, g, slot_out);
+        return relax<P>(tab, mask, max_probe, key, g, prev, slot_out);
 }
 
 __device__ __forceinline__ Cand load_cand(const Cand *p) {
@@ -590,7 +604,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
             const Key key0 = prob.start_key();
             const uint32_t aux0 = prob.start_aux();
             uint32_t s0;
-            if (relax_key<P>(m.tab, m.mask, m.max_probe, key0, 0, &s0) == RELAX_FULL) {
+            if (relax_key<P>(m.tab, m.mask, m.max_probe, key0, 0, kNone, &s0) == RELAX_FULL) {
                 set_error(&st->error, ST_HASH_FULL);
             } else {
                 P::set_link(m.tab + s0, kNone, aux0);
@@ -771,7 +785,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                     prob.succ_begin(pi.key, pi.g, pi.aux, move, sc);
                     ng = sc.g;
                     ++nS;
-                    const int r = relax_key<P>(m.tab, m.mask, m.max_probe, sc.key, sc.g, &nslot);
+                    const int r = relax_key<P>(m.tab, m.mask, m.max_probe, sc.key, sc.g, oslot, &nslot);
                     prob.succ_end(sc, pi.aux, move, naux, nf);
                     if (r == RELAX_FULL) {
                         set_error(&st->err[r3], ST_HASH_FULL);
@@ -885,11 +899,15 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
             }
             const Cand c = load_cand(half + (size_t)lo * RR + 1 + (i - roff[lo]));
             E e = prob.make_entry(c.f, c.g, c.slot, c.aux);
-            if (P::slot_g(m.tab + c.slot) == c.g) {
-                P::set_link(m.tab + c.slot, c.parent, c.aux);
-            } else {
-                e.slot = kNone;  // lost to a better writer
+            if constexpr (!P::kPrevInKey) {
+                if (P::slot_g(m.tab + c.slot) == c.g)
+                    P::set_link(m.tab + c.slot, c.parent, c.aux);
+                else
+                    e.slot = kNone;  // lost to a better writer
             }
+            // (link in the key word: every candidate is pushed; one that lost
+            // to a better writer of the round is a stale entry, dropped when
+            // popped, and at most one candidate per slot carries its final g)
             stage[q] = e;
         }
         __syncthreads();

@@ -105,8 +105,11 @@ __global__ void k_noalloc_finish(const unsigned char *scratch, int32_t *path, in
             r.diagonal = (int64_t)(gbest & 0xffffffffu);
             uint32_t s = __ldcg(&st->goal_slot);
             while (s != kNone && n < cap) {
-                path[n++] = (int32_t)__ldcg(&tab[s].key);
-                s = __ldcg(&tab[s].prev);
+                uint64_t key;
+                uint32_t prev;
+                slot_key_prev(tab + s, GridProblem::kPrevInKey, key, prev);
+                path[n++] = (int32_t)key;
+                s = prev;
             }
             if (s != kNone) {
                 r.status = UASTAR_ARENA_FULL;  // the caller's path buffer is too small
