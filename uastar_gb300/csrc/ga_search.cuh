@@ -723,9 +723,9 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
             if (lane == 31) scratch[2 + (tid >> 5)] = incl;
         }
         __syncthreads();
+        uint64_t cmin = kInfCost;  // the CTA's minimum popped f (thread 0)
         if (tid == 0) {
             uint32_t acc = 0;
-            uint64_t cmin = kInfCost;
             for (uint32_t w = 0; w < owner_warps; ++w) {
                 const uint32_t t = scratch[2 + w];
                 scratch[2 + w] = acc;
@@ -733,12 +733,13 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                 if (P::cost_cmp(wmins[w], cmin) < 0) cmin = wmins[w];
             }
             scratch[0] = acc;
-            if (cmin != kInfCost) atomic_min_cost<P>(&st->round_min[r3], cmin);
         }
         __syncthreads();
         if (owner) pop[tid].excl += scratch[2 + (tid >> 5)];
         const uint32_t total = scratch[0];
         __syncthreads();
+        // into the team's round minimum, off the pop's path (before the barrier)
+        if (tid == 0 && cmin != kInfCost) atomic_min_cost<P>(&st->round_min[r3], cmin);
 
         // ------------------ phase 1: relax successors / refill heap roots ---
         // Owner chores of the round, while the other warps relax: refill the
@@ -829,6 +830,10 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         // Every value read here was written before the barrier above and is
         // not written again before every CTA has read it (see TeamState), so
         // all threads decide alike.
+        // the push phase's region counts, read beside the decision's words
+        const uint32_t per = (C + T - 1) / T, rb = tid * per, re = min(rb + per, C);
+        const uint32_t pre0 = rb < re ? ldcg_u32(&half[(size_t)rb * RR].slot) : 0u;
+        const uint32_t pre1 = rb + 1 < re ? ldcg_u32(&half[(size_t)(rb + 1) * RR].slot) : 0u;
         const uint64_t rmin = team.rd64(&st->round_min[r3]);
         const uint64_t gmin = team.rd64(&st->goal_min[r3]);
         if (P::cost_cmp(gmin, gbest) < 0) gbest = gmin;
@@ -871,10 +876,9 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         // winners write prev/aux and are staged for their heap's owner.
         // The round's candidates are numbered region by region: offsets of the
         // C regions (each thread sums `per` consecutive regions' counts).
-        const uint32_t per = (C + T - 1) / T, rb = tid * per, re = min(rb + per, C);
         uint32_t mine = 0;
         for (uint32_t r = rb; r < re; ++r) {
-            const uint32_t n = ldcg_u32(&half[(size_t)r * RR].slot);
+            const uint32_t n = r == rb ? pre0 : r == rb + 1 ? pre1 : ldcg_u32(&half[(size_t)r * RR].slot);
             roff[r] = n;
             mine += n;
         }
