@@ -229,6 +229,8 @@ typedef struct {
     int32_t use_graph;            /* launch through a captured CUDA graph (default 1) */
     int32_t tier1_rounds;         /* round budget of a single-CTA team (0 -> 2048) */
     int32_t tier2_puzzle_rounds;  /* round budget of a puzzle on a cluster team (0 -> 16384) */
+    int32_t cluster_size;         /* CTAs per cluster team (0 -> 8; 2..16) */
+    int32_t reserved;
 } uastar_batch_config;
 
 typedef struct {

@@ -67,7 +67,8 @@ class InstanceResult(C.Structure):
 class BatchConfig(C.Structure):
     _fields_ = [("threads_per_instance", C.c_int32), ("threads_per_heap", C.c_int32),
                 ("heap_capacity", C.c_int32), ("load_factor", C.c_double), ("ctas", C.c_int32),
-                ("use_graph", C.c_int32), ("tier1_rounds", C.c_int32), ("tier2_puzzle_rounds", C.c_int32)]
+                ("use_graph", C.c_int32), ("tier1_rounds", C.c_int32), ("tier2_puzzle_rounds", C.c_int32),
+                ("cluster_size", C.c_int32), ("reserved", C.c_int32)]
 
 
 class BatchStats(C.Structure):

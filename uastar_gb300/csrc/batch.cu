@@ -854,7 +854,8 @@ int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int
         bool heap_over = false;
         for (int i : tier2) heap_over |= results[i].status == UASTAR_HEAP_OVERFLOW;
         if (heap_over) gc.set_capacity(g.want * 16 + 15);
-        rc = resolve_cluster_geometry(eng, 8, &gc);
+        const int csize = cfg && cfg->cluster_size >= 2 && cfg->cluster_size <= 16 ? cfg->cluster_size : 8;
+        rc = resolve_cluster_geometry(eng, csize, &gc);
         if (rc) return rc;
         std::vector<int> m(tier2.size());
         for (size_t j = 0; j < tier2.size(); ++j) m[j] = mult[tier2[j]] * 2;

@@ -326,13 +326,13 @@ class Engine:
     # batched engine
     def batch_solve(self, instances: Iterable, *, threads_per_instance: int = 0, threads_per_heap: int = 0,
                     heap_capacity: int = 0, load_factor: float = 0.0, ctas: int = 0, use_graph: int = 1,
-                    tier1_rounds: int = 0, tier2_puzzle_rounds: int = 0):
+                    tier1_rounds: int = 0, tier2_puzzle_rounds: int = 0, cluster_size: int = 0):
         insts = list(instances)
         keep: list = []
         arr = (L.Instance * max(1, len(insts)))(*[_to_struct(i, keep) for i in insts])
         res = (L.InstanceResult * max(1, len(insts)))()
         cfg = L.BatchConfig(threads_per_instance, threads_per_heap, heap_capacity, load_factor, ctas, use_graph,
-                            tier1_rounds, tier2_puzzle_rounds)
+                            tier1_rounds, tier2_puzzle_rounds, cluster_size, 0)
         st = L.BatchStats()
         self._check(self._lib.uastar_batch_solve(self._h, arr, len(insts), C.byref(cfg), res, C.byref(st)),
                     "batch_solve")
