@@ -4,6 +4,8 @@
     python -m uastar_gb300.cases grid_20000 [--repeat 2]
     python -m uastar_gb300.cases puzzle15 [--count 10]
     python -m uastar_gb300.cases mixed_small [--repeat 1]
+    python -m uastar_gb300.cases cluster_small [--repeat 1]
+    python -m uastar_gb300.cases pdb4 [--repeat 1]
 
 Each repeat solves the case once and prints one line of results; profilers
 capture the second launch of the search kernel (`-s 1 -c 1`).
@@ -19,7 +21,7 @@ from . import workloads as WL
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["grid_1000", "grid_20000", "puzzle15", "mixed_small"])
+    ap.add_argument("case", choices=["grid_1000", "grid_20000", "puzzle15", "mixed_small", "cluster_small", "pdb4"])
     ap.add_argument("--repeat", type=int, default=2)
     ap.add_argument("--count", type=int, default=10)
     args = ap.parse_args()
@@ -41,6 +43,22 @@ def main() -> None:
                 t0 = time.perf_counter()
                 steps = [eng.puzzle_solve(4, s.tiles()).steps for s in WL.puzzle15_x100(count=args.count)]
                 print(f"puzzle15: {len(steps)} solves in {time.perf_counter() - t0:.3f} s, steps {steps}", flush=True)
+    elif args.case == "pdb4":
+        with Engine(0) as eng:
+            for _ in range(args.repeat):
+                print(f"pdb4: built in {eng.pdb_build(4):.1f} ms", flush=True)
+    elif args.case == "cluster_small":
+        # 36 15-puzzles of 120-move walks and 4 grids of 2200^2: a 64-round
+        # budget on the single-CTA tier sends most of them to 8-CTA clusters
+        specs = [WL.PuzzleSpec(4, 120, 8000 + i) for i in range(36)]
+        specs += [WL.screened_grid(2200, 2200, 0.25, 21 + i, exact=True) for i in range(4)]
+        insts = [s.instance() for s in specs]
+        with Engine(0) as eng:
+            eng.pdb_build(4)
+            for _ in range(args.repeat):
+                res, st = eng.batch_solve(insts, tier1_rounds=64)
+                print(f"cluster_small: {sum(r['status'] == 0 for r in res)}/{len(res)} ok, "
+                      f"{st['wall_ms']:.1f} ms, waves {st['waves']}", flush=True)
     else:
         specs = [WL.PuzzleSpec(4, 60 + i, 7000 + i) for i in range(48)]
         specs += [WL.screened_grid(256 + 32 * i, 256 + 32 * i, 0.25, 11 + i, exact=True) for i in range(8)]
