@@ -538,8 +538,7 @@ bool board_solvable(int n, const uint8_t *tiles) {
 }
 
 template <int N>
-int32_t puzzle_solve_n(uastar_engine *eng, const uint8_t *tiles, uastar_puzzle_result *out,
-                       PlainOut *po) {
+int32_t puzzle_solve_n(uastar_engine *eng, const uint8_t *tiles, PlainOut *po) {
     PuzzleProblem<N> prob;
     prob.pdb = eng->pdb[N].as<uint8_t>();
     prob.start = pack_board(N, tiles);
@@ -549,7 +548,7 @@ int32_t puzzle_solve_n(uastar_engine *eng, const uint8_t *tiles, uastar_puzzle_r
 
 // 5x5: 16-byte keys (PuzzleProblem<5>)
 template <>
-int32_t puzzle_solve_n<5>(uastar_engine *eng, const uint8_t *tiles, uastar_puzzle_result *, PlainOut *po) {
+int32_t puzzle_solve_n<5>(uastar_engine *eng, const uint8_t *tiles, PlainOut *po) {
     PuzzleProblem<5> prob;
     prob.pdb = eng->pdb[5].as<uint8_t>();
     prob.start = PuzzleProblem<5>::pack(tiles);
@@ -779,9 +778,9 @@ int32_t uastar_puzzle_solve(uastar_engine *eng, int32_t n, const uint8_t *tiles,
         return out->status;
     }
     PlainOut po;
-    int32_t rc = n == 3   ? puzzle_solve_n<3>(eng, tiles, out, &po)
-                 : n == 4 ? puzzle_solve_n<4>(eng, tiles, out, &po)
-                          : puzzle_solve_n<5>(eng, tiles, out, &po);
+    int32_t rc = n == 3   ? puzzle_solve_n<3>(eng, tiles, &po)
+                 : n == 4 ? puzzle_solve_n<4>(eng, tiles, &po)
+                          : puzzle_solve_n<5>(eng, tiles, &po);
     if (rc) return out->status = rc;
     const TeamState &st = po.st;
     out->status = (int32_t)st.status;
