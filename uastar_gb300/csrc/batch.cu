@@ -869,9 +869,17 @@ int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int
         if (rc) return rc;
         todo = retry;
     }
-    // the partitions of a large batch can hold a large share of HBM: return them
-    eng->b_tab.release();
-    eng->b_bitmaps.release();
+    // The team regions are kept for the next batch (teams x region, tens of
+    // GB at most); only a plain-engine escalation that finds too little free
+    // memory for its table gets them back.
+    if (!todo.empty()) {
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        if (free_b < (32ull << 30)) {
+            eng->b_tab.release();
+            eng->b_bitmaps.release();
+        }
+    }
     for (int i : todo) {
         const uastar_instance &in = insts[i];
         uastar_instance_result &r = results[i];
