@@ -460,7 +460,9 @@ def main():
     eng, line = run_ours(args, rank, world, local_rank)
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(args)
-        if not args.headline_only:
+        # The single-GPU sections run at N = 1 only: a replica run measures
+        # the headline, without holding N GPUs for minutes more.
+        if not args.headline_only and world == 1:
             # The other workloads run on an engine with the default (automatic)
             # configuration, which is what a caller of the plain, batched and
             # serving entry points gets; the headline engine's fixed 2^28-slot
