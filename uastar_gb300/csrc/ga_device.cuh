@@ -225,7 +225,7 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 
 // ------------------------------------------------------------- barrier ---
 // Grid-wide barrier for a cooperative launch.  The arrival counter only grows
-// (one atomicAdd per CTA per barrier, no reset), so barrier number e is
+// (one release add per CTA per barrier, no reset), so barrier number e is
 // complete when the counter reaches e * nblocks (compared modulo 2^32).
 // Thread 0 of each CTA waits with a time bound: when it expires, or when
 // another CTA has flagged an error, it records ST_TIMEOUT (first error wins)
@@ -237,8 +237,9 @@ __device__ __forceinline__ void grid_barrier(uint32_t *counter, uint32_t nblocks
     if (threadIdx.x == 0) {
         epoch += 1;
         const uint32_t target = epoch * nblocks;
-        __threadfence();
-        atomicAdd(counter, 1u);
+        // release at GPU scope: cumulative over the CTA's writes, which the
+        // CTA barrier above ordered before this thread's arrival
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(counter) : "memory");
         const uint64_t t0 = globaltimer_ns();
         uint32_t spins = 0;
         while ((int32_t)(ld_acquire_u32(counter) - target) < 0) {
@@ -250,7 +251,8 @@ __device__ __forceinline__ void grid_barrier(uint32_t *counter, uint32_t nblocks
                 }
             }
         }
-        __threadfence();
+        // the acquire load that saw the last arrival orders this thread after
+        // every CTA's release; the CTA barrier below carries that to the rest
     }
     __syncthreads();
 }
