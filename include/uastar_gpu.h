@@ -67,6 +67,13 @@ typedef struct {
     double wait_timeout_s;   /* bound on any device-side barrier wait (0 -> 10 s) */
     int32_t threads_per_heap; /* threads that share one heap's successors (0 -> 4) */
     int32_t heap_top_levels;  /* heap levels kept in shared memory (0 -> as many as fit, -1 -> none) */
+    int32_t dedup;            /* removal of a round's duplicate grid successors: 0 -> the dedup
+                                 table keeps the minimum g with a CAS loop (default); 1 -> the
+                                 reference's order (src/pathway/GPU-solver.cu:218-235): the round's
+                                 successors are radix-sorted by cell on the device and each cell's
+                                 least-g record is relaxed once.  Same results; puzzles always use 0
+                                 (the reference's puzzle kernel probes its table per successor) */
+    int32_t reserved;
 } uastar_config;
 
 /* Replaces GPUPathwaySolver/GPUPuzzleSolver construction + initialize()'s
@@ -121,6 +128,15 @@ int32_t uastar_grid_solve(uastar_engine *eng, const uint64_t *words, int32_t H, 
  * GPU-kernel.cuh:546-569).  Returns the path length (>= 0, may exceed cap,
  * only cap ids are written) or -status on failure. */
 int64_t uastar_grid_path(uastar_engine *eng, int32_t *ids, int64_t cap);
+
+/* The device sort of the sorted dedup mode (uastar_config.dedup = 1), which
+ * replaces the reference's per-round MergesortPairs of the successor list
+ * (src/pathway/GPU-solver.cu:218), run on its own: a stable LSD radix sort of
+ * n 32-bit keys on key bits [0, key_bits) (0 -> 32; every key must be below
+ * 2^key_bits) by the whole GPU as one team.  perm[j] = position of the j-th
+ * smallest key, equal keys in position order.  0 <= n <= 2048 x SMs. */
+int32_t uastar_sort_keys(uastar_engine *eng, const uint32_t *keys, int64_t n, int32_t key_bits,
+                         uint32_t *perm);
 
 /* ---- sliding-tile puzzle (--puzzle) ----------------------------------- */
 typedef struct {

@@ -34,7 +34,7 @@ def test_bindings_cover_header():
 
 def test_struct_sizes_match_c_layout():
     # sizes computed from the header's field lists (natural alignment, x86-64 / aarch64)
-    assert C.sizeof(L.Config) == 48
+    assert C.sizeof(L.Config) == 56
     assert C.sizeof(L.GridResult) == 104
     assert C.sizeof(L.PuzzleResult) == 72
     assert C.sizeof(L.Instance) == 64

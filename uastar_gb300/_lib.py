@@ -27,7 +27,8 @@ KIND_GRID, KIND_PUZZLE = 1, 2
 class Config(C.Structure):
     _fields_ = [("heaps", C.c_int32), ("block_threads", C.c_int32), ("heap_capacity", C.c_int32),
                 ("hash_log2_slots", C.c_int32), ("max_load", C.c_double), ("max_rounds", C.c_int64),
-                ("wait_timeout_s", C.c_double), ("threads_per_heap", C.c_int32), ("heap_top_levels", C.c_int32)]
+                ("wait_timeout_s", C.c_double), ("threads_per_heap", C.c_int32), ("heap_top_levels", C.c_int32),
+                ("dedup", C.c_int32), ("reserved", C.c_int32)]
 
 
 class GridResult(C.Structure):
@@ -120,6 +121,7 @@ SIGNATURES = [
     ("uastar_grid_solve", C.c_int32, [_P, _U64P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                       C.c_int32, C.POINTER(GridResult)]),
     ("uastar_grid_path", C.c_int64, [_P, _I32P, C.c_int64]),
+    ("uastar_sort_keys", C.c_int32, [_P, C.POINTER(C.c_uint32), C.c_int64, C.c_int32, C.POINTER(C.c_uint32)]),
     ("uastar_pdb_build", C.c_int32, [_P, C.c_int32, _DP]),
     ("uastar_pdb_bytes", C.c_int64, [C.c_int32]),
     ("uastar_pdb_load", C.c_int32, [_P, C.c_int32, _U8P, C.c_int64]),

@@ -1,7 +1,7 @@
 """Run one named workload case on the engine (for profiling and quick checks).
 
     python -m uastar_gb300.cases grid_1000 [--repeat 2]
-    python -m uastar_gb300.cases grid_20000 [--repeat 2]
+    python -m uastar_gb300.cases grid_20000 [--repeat 2] [--dedup 1]
     python -m uastar_gb300.cases puzzle15 [--count 10]
     python -m uastar_gb300.cases mixed_small [--repeat 1]
     python -m uastar_gb300.cases cluster_small [--repeat 1]
@@ -24,18 +24,19 @@ def main() -> None:
     ap.add_argument("case", choices=["grid_1000", "grid_20000", "puzzle15", "mixed_small", "cluster_small", "pdb4"])
     ap.add_argument("--repeat", type=int, default=2)
     ap.add_argument("--count", type=int, default=10)
+    ap.add_argument("--dedup", type=int, default=0, help="grids: 0 table minimum, 1 per-round sort + unique")
     args = ap.parse_args()
 
     if args.case in ("grid_1000", "grid_20000"):
         sp = WL.GRID_1000 if args.case == "grid_1000" else WL.GRID_20000
         # fixed tables: one search launch per solve (no in-place growth)
-        kw = {"hash_log2_slots": 28 if args.case == "grid_20000" else 22}
+        kw = {"hash_log2_slots": 28 if args.case == "grid_20000" else 22, "dedup": args.dedup}
         words = sp.words()
         with Engine(0, heaps=8192, block_threads=256, threads_per_heap=4, **kw) as eng:
             for _ in range(args.repeat):
                 r = eng.grid_solve(words, sp.H, sp.W, sp.start, sp.goal)
                 print(f"{args.case}: {r.straight}+{r.diagonal}*sqrt2 cost {r.cost:.4f} expanded {r.expanded} "
-                      f"rounds {r.rounds} kernel {r.kernel_ms:.1f} ms", flush=True)
+                      f"generated {r.generated} rounds {r.rounds} kernel {r.kernel_ms:.1f} ms", flush=True)
     elif args.case == "puzzle15":
         with Engine(0, hash_log2_slots=25) as eng:  # fixed table: one launch per solve
             eng.pdb_build(4)

@@ -29,12 +29,35 @@ __global__ void k_fill_ff(uint4 *p, size_t n16) {
         p[i] = v;
 }
 
-template <class P>
+template <class P, bool kSort = false>
 __global__ void __launch_bounds__(512, 1) k_plain_search(P prob, SearchMem<typename P::Entry> m,
                                                       TeamState *st, uint64_t timeout_ns, uint32_t H) {
     extern __shared__ __align__(128) unsigned char smem[];
     GridTeam team{st, 0u, timeout_ns};
-    ga_search<P>(prob, team, m, H, smem, ~0ull);
+    ga_search<P, GridTeam, kSort>(prob, team, m, H, smem, ~0ull);
+}
+
+// The search kernel of a plain solve: the sorted-dedup variant exists for
+// grids only.
+template <class P> const void *plain_kernel(bool sorted) {
+    if constexpr (std::is_same<P, GridProblem>::value)
+        if (sorted) return (const void *)k_plain_search<P, true>;
+    return (const void *)k_plain_search<P, false>;
+}
+
+// Stand-alone run of the search's team sort (uastar_sort_keys): the whole
+// grid as one team sorts n keys (n <= gridDim.x * blockDim.x * 8) and writes
+// the stable permutation.
+__global__ void __launch_bounds__(256, 1) k_team_sort(const uint32_t *keys, uint32_t n, uint32_t bits,
+                                                      unsigned long long *buf, uint32_t *hist, uint32_t *perm,
+                                                      TeamState *st, uint64_t timeout_ns) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    GridTeam team{st, 0u, timeout_ns};
+    const unsigned long long *out = team_radix_sort<8>(
+        team, n, bits, [&](uint32_t i) { return __ldg(keys + i); }, buf, buf + n, hist,
+        reinterpret_cast<uint32_t *>(smem), &st->error);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        perm[i] = (uint32_t)__ldcg(out + i);
 }
 
 // The best open node of a paused puzzle search: the minimum entry (least f,
@@ -218,6 +241,18 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
     int log2 = c.hash_log2_slots > 0 ? c.hash_log2_slots : log2_auto;
     if (max_log2 > 0) log2 = std::min(log2, max_log2);
     uint32_t stride = c.heap_capacity > 0 ? next_pow2_u32((uint32_t)c.heap_capacity + 1) : stride_auto;
+    if (c.dedup != 0 && c.dedup != 1) {
+        eng->set_err("dedup must be 0 (table minimum) or 1 (sorted)");
+        return UASTAR_BAD_INPUT;
+    }
+    bool sorted = false;
+    uint32_t sort_bits = 0;
+    if constexpr (std::is_same<P, GridProblem>::value) {
+        sorted = c.dedup == 1;
+        sort_bits = (uint32_t)std::max(1, ceil_log2_u64((uint64_t)prob.H * (uint64_t)prob.W));
+    }
+    const void *kfn = plain_kernel<P>(sorted);
+    const size_t sort_extra = sorted ? sort_smem_bytes(block) + 16 : 0;
 
     // shared heap tops: as many levels as fit while the whole team stays
     // co-resident (ceil(nblocks / SMs) CTAs per SM)
@@ -226,12 +261,12 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, eng->device);
     const int per_sm = (int)((nblocks + eng->sms - 1) / eng->sms);
     const size_t smem_budget = (size_t)std::max(8 * 1024, std::min(smem_optin, smem_sm / std::max(1, per_sm) - 2048));
-    const uint32_t L = fit_levels<P>(H, c.heap_top_levels, smem_budget);
-    const size_t smem = SearchSmem<P>::bytes(H, L);
-    cudaError_t e = cudaFuncSetAttribute(k_plain_search<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const uint32_t L = fit_levels<P>(H, c.heap_top_levels, smem_budget - sort_extra);
+    const size_t smem = sorted ? SearchSmem<P>::bytes_sorted(H, L, block) : SearchSmem<P>::bytes(H, L);
+    cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return fail_cuda(eng, e, "smem attribute");
     int max_active = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_active, k_plain_search<P>, (int)block, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_active, kfn, (int)block, smem);
     if (e != cudaSuccess) return fail_cuda(eng, e, "occupancy");
     if (nblocks + 1 > 32 * H) {  // the push phase keeps nblocks + 1 region offsets in shared memory
         eng->set_err("too many CTAs for the heaps per CTA (need CTAs < 32 * block_threads / threads_per_heap)");
@@ -255,6 +290,9 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
         if ((e = eng->heap_size.ensure((size_t)k * 4)) != cudaSuccess) return fail_cuda(eng, e, "alloc heap sizes");
         if ((e = eng->cand.ensure(cand_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc candidates");
         if ((e = eng->team.ensure(sizeof(TeamState))) != cudaSuccess) return fail_cuda(eng, e, "alloc state");
+        const uint64_t sort_n = (uint64_t)k * P::kMoves;  // a round's successors at most
+        if (sorted && (e = eng->sortb.ensure(2 * sort_n * 8 + 256ull * (nblocks + 1) * 4)) != cudaSuccess)
+            return fail_cuda(eng, e, "alloc sort buffers");
 
         int32_t rc = fill_ff(eng, eng->tab.p, tab_b);
         if (rc) return rc;
@@ -277,6 +315,11 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
         m.heap_size = eng->heap_size.as<uint32_t>();
         m.cand = eng->cand.as<Cand>();
         m.max_rounds = (uint64_t)c.max_rounds;
+        if (sorted) {
+            m.sort_buf = eng->sortb.as<unsigned long long>();
+            m.sort_hist = reinterpret_cast<uint32_t *>(m.sort_buf + 2 * sort_n);
+            m.sort_bits = sort_bits;
+        }
         // an auto-sized table grows in place (x4) when half full; at the cap
         // the search pauses instead, two rounds' worth of inserts short of
         // the load limit
@@ -291,8 +334,7 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
         for (;;) {
             void *args[] = {&pr, &m, &st, &timeout_ns, &h_arg};
             cudaEventRecord(eng->ev0, eng->stream);
-            e = cudaLaunchCooperativeKernel((const void *)k_plain_search<P>, dim3(nblocks), dim3(block),
-                                            args, smem, eng->stream);
+            e = cudaLaunchCooperativeKernel(kfn, dim3(nblocks), dim3(block), args, smem, eng->stream);
             if (e != cudaSuccess) return fail_cuda(eng, e, "cooperative launch");
             eng->launches++;
             cudaEventRecord(eng->ev1, eng->stream);
@@ -695,6 +737,7 @@ void uastar_destroy(uastar_engine *eng) {
     cudaSetDevice(eng->device);
     cudaStreamSynchronize(eng->stream);
     for (DevBuf *b : {&eng->tab, &eng->heaps, &eng->heap_size, &eng->cand, &eng->team, &eng->walk,
+                      &eng->tab_next, &eng->grow_map, &eng->sortb,
                       &eng->bitmap, &eng->b_desc, &eng->b_out, &eng->b_queue, &eng->b_bitmaps,
                       &eng->b_tab, &eng->b_heaps, &eng->b_hsize, &eng->b_cand, &eng->b_walk,
                       &eng->b_walklen, &eng->b_cstate, &eng->b_cnext})
@@ -707,6 +750,60 @@ void uastar_destroy(uastar_engine *eng) {
 }
 
 const char *uastar_last_error(const uastar_engine *eng) { return eng ? eng->err.c_str() : "null engine"; }
+
+int32_t uastar_sort_keys(uastar_engine *eng, const uint32_t *keys, int64_t n, int32_t key_bits, uint32_t *perm) {
+    if (!eng) return UASTAR_BAD_INPUT;
+    constexpr uint32_t T = 256, kPer = 8;
+    const uint64_t C = (uint64_t)std::max(1, eng->sms);
+    if (n < 0 || (n > 0 && (!keys || !perm)) || key_bits < 0 || key_bits > 32) {
+        eng->set_err("sort: bad arguments");
+        return UASTAR_BAD_INPUT;
+    }
+    if ((uint64_t)n > C * T * kPer) {
+        eng->set_err("sort: more than 2048 keys per SM");
+        return UASTAR_BAD_INPUT;
+    }
+    const uint32_t bits = key_bits == 0 ? 32u : (uint32_t)key_bits;
+    if (bits < 32)
+        for (int64_t i = 0; i < n; ++i)
+            if (keys[i] >> bits) {
+                eng->set_err("sort: a key has bits above key_bits");
+                return UASTAR_BAD_INPUT;
+            }
+    if (n == 0) return UASTAR_OK;
+    cudaSetDevice(eng->device);
+    const size_t nn = (size_t)n;
+    const size_t bytes = nn * 4 + nn * 4 + 2 * nn * 8 + 256 * (C + 1) * 4 + 64;
+    cudaError_t e;
+    if ((e = eng->sortb.ensure(bytes)) != cudaSuccess) return fail_cuda(eng, e, "alloc sort");
+    if ((e = eng->team.ensure(sizeof(TeamState))) != cudaSuccess) return fail_cuda(eng, e, "alloc state");
+    unsigned long long *buf = eng->sortb.as<unsigned long long>();
+    uint32_t *d_keys = reinterpret_cast<uint32_t *>(buf + 2 * nn);
+    uint32_t *d_perm = d_keys + nn;
+    uint32_t *hist = d_perm + nn;
+    TeamState *st = eng->team.as<TeamState>();
+    TeamState init = fresh_team_state();
+    if ((e = cudaMemcpyAsync(st, &init, sizeof init, cudaMemcpyHostToDevice, eng->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(d_keys, keys, nn * 4, cudaMemcpyHostToDevice, eng->stream)) != cudaSuccess)
+        return fail_cuda(eng, e, "sort upload");
+    uint32_t n32 = (uint32_t)n, bits_arg = bits;
+    uint64_t timeout_ns = (uint64_t)(eng->cfg.wait_timeout_s * 1e9);
+    void *args[] = {&d_keys, &n32, &bits_arg, &buf, &hist, &d_perm, &st, &timeout_ns};
+    e = cudaLaunchCooperativeKernel((const void *)k_team_sort, dim3((unsigned)C), dim3(T), args,
+                                    sort_smem_bytes(T), eng->stream);
+    if (e != cudaSuccess) return fail_cuda(eng, e, "sort launch");
+    eng->launches++;
+    uint32_t err = 0;
+    if ((e = cudaMemcpyAsync(perm, d_perm, nn * 4, cudaMemcpyDeviceToHost, eng->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(&err, &st->error, 4, cudaMemcpyDeviceToHost, eng->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(eng->stream)) != cudaSuccess)
+        return fail_cuda(eng, e, "sort");
+    if (err) {
+        eng->set_err("sort: a team barrier gave up");
+        return UASTAR_TIMEOUT;
+    }
+    return UASTAR_OK;
+}
 
 int32_t uastar_set_stream(uastar_engine *eng, void *cuda_stream) {
     if (!eng) return UASTAR_BAD_INPUT;

@@ -57,6 +57,7 @@ struct uastar_engine {
     // plain engine buffers
     uastar::DevBuf tab, heaps, heap_size, cand, team, walk, bitmap;
     uastar::DevBuf tab_next, grow_map;  // table growth of a paused search
+    uastar::DevBuf sortb;               // per-round successor sort (dedup = 1), uastar_sort_keys
     int32_t gH = 0, gW = 0;
     bool grid_loaded = false;
     // pattern databases, indexed by board side

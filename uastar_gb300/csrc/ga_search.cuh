@@ -49,6 +49,7 @@
 #include <cstdint>
 
 #include "ga_device.cuh"
+#include "ga_sort.cuh"
 
 namespace uastar {
 
@@ -69,6 +70,11 @@ template <class E> struct SearchMem {
     // and no work in flight, so that the host can move the table to a larger
     // one and resume; ~0 = never.
     uint64_t grow_at = ~0ull;
+    // Sort-based dedup (ga_search<.., true>): every round's successors are
+    // radix-sorted by key and each key's minimum-g record is relaxed once.
+    unsigned long long *sort_buf = nullptr;  // 2 x C * H * kMoves pairs
+    uint32_t *sort_hist = nullptr;           // 256 x (C + 1) digit counts
+    uint32_t sort_bits = 0;                  // key bits to sort on
 };
 
 // ------------------------------------------------------------------ teams ---
@@ -521,6 +527,11 @@ template <class P> struct SearchSmem {
     static __host__ __device__ size_t bytes(uint32_t H, uint32_t L) {
         return scratch_offset(H, L) + 4 * kScratchWords;
     }
+    // the sort-based dedup's shared memory follows (T threads per CTA)
+    static __host__ __device__ size_t sort_offset(uint32_t H, uint32_t L) { return (bytes(H, L) + 15) & ~(size_t)15; }
+    static __host__ __device__ size_t bytes_sorted(uint32_t H, uint32_t L, uint32_t T) {
+        return sort_offset(H, L) + sort_smem_bytes(T);
+    }
 };
 
 // Exclusive prefix sum over the CTA of one value per thread (blockDim.x a
@@ -557,10 +568,20 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *scratc
 // and the table).  Returns ST_RUNNING if the budget ran out first or the
 // table passed m.grow_at, else the final status.  Every thread of every CTA of the team must call it with the
 // same H (heaps per CTA, 1 <= H <= blockDim.x); `smem` points at
-// SearchSmem<P>::bytes(H, m.L) bytes of shared memory (128-byte aligned).
-template <class P, class Team>
+// SearchSmem<P>::bytes(H, m.L) bytes of shared memory (128-byte aligned),
+// bytes_sorted(H, m.L, blockDim.x) with kSort.
+//
+// kSort (keys of at most 32 bits) runs the reference's dedup order instead
+// of the in-table minimum: the relax phase only writes every successor's
+// record; after the decision the team radix-sorts the round's records by key
+// (team_radix_sort), and the first record of each key's run with the least g
+// (the sort is stable: the earliest of equal g) is relaxed into the table,
+// once per key, and pushed if it strictly improved the slot.  Same result,
+// three team barriers per sort pass more per round.
+template <class P, class Team, bool kSort = false>
 __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typename P::Entry> &m, uint32_t H,
                               unsigned char *smem, uint64_t budget) {
+    static_assert(!kSort || (!P::kWide && P::kPrevInKey), "sorted dedup: 32-bit keys with the link in the key word");
     using E = typename P::Entry;
     TeamState *st = team.st;
     const uint32_t T = blockDim.x, tid = threadIdx.x, lane = tid & 31u;
@@ -636,6 +657,8 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
     const uint64_t RR = cand_region_records<P>(H);
     uint32_t *const s_cnt = scratch + 36;  // this CTA's candidates this round
     uint32_t *const s_ins = scratch + 37;  // dedup slots it claimed this round
+    uint32_t *const s_ins2 = scratch + 38;  // (kSort) slots claimed after the sort
+    uint32_t *const ssm = reinterpret_cast<uint32_t *>(smem + SearchSmem<P>::sort_offset(H, L));
     unsigned long long *const wmins = reinterpret_cast<unsigned long long *>(scratch + 40);  // per owner warp
     // Push-phase staging: one entry per candidate of this CTA's share (at most
     // H * kMoves), then the C + 1 region offsets of the round's candidates
@@ -651,6 +674,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         if (tid == 0) {
             *s_cnt = 0;
             *s_ins = 0;
+            *s_ins2 = 0;
         }
 
         // ------------------------------------------------ phase 1: pop ---
@@ -762,7 +786,37 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
             }
         };
         if (rfirst > 0 && owner) chores();
-        if (relaxer) {
+        if constexpr (kSort) {
+            // every successor's record, at its number in the CTA's list
+            if (relaxer) {
+                for (uint32_t j = tid - rfirst; j < total; j += rthreads) {
+                    uint32_t lo = 0, hi = H - 1;
+                    while (lo < hi) {
+                        const uint32_t mid = (lo + hi + 1) >> 1;
+                        if (pop[mid].excl <= j)
+                            lo = mid;
+                        else
+                            hi = mid - 1;
+                    }
+                    const PopInfo<Key> &pi = pop[lo];
+                    const int move = (int)__fns(pi.mask, 0, (int)(j - pi.excl) + 1);
+                    typename P::Succ sc;
+                    prob.succ_begin(pi.key, pi.g, pi.aux, move, sc);
+                    uint32_t naux;
+                    uint64_t nf;
+                    prob.succ_end(sc, pi.aux, move, naux, nf);
+                    ++nS;
+                    Cand c;
+                    c.slot = (uint32_t)sc.key;
+                    c.parent = pi.slot;
+                    c.g = sc.g;
+                    c.f = nf;
+                    c.aux = naux;
+                    c.pad = 0;
+                    myreg[j] = c;
+                }
+            }
+        } else if (relaxer) {  // (not kSort)
             const uint32_t rt = tid - rfirst;
             for (uint32_t b0 = 0; b0 < total; b0 += rthreads) {
                 const uint32_t j = b0 + rt;
@@ -821,7 +875,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         // publish this CTA's round: its candidate count and claimed slots
         __syncthreads();
         if (tid == 0) {
-            half[(size_t)cta * RR].slot = *s_cnt;
+            half[(size_t)cta * RR].slot = kSort ? total : *s_cnt;
             if (*s_ins) atomicAdd(&st->ins[r3], (unsigned long long)*s_ins);
         }
         team.sync();
@@ -891,8 +945,8 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         }
         __syncthreads();
         const uint32_t nshare = ncand > cta ? (ncand - cta + C - 1) / C : 0u;
-        for (uint32_t q = tid; q < nshare; q += T) {
-            const uint32_t i = cta + C * q;
+        // the region record of the round's candidate number i
+        const auto rec = [&](uint32_t i) -> const Cand * {
             uint32_t lo = 0, hi = C - 1;  // the last region starting at or before i
             while (lo < hi) {
                 const uint32_t mid = (lo + hi + 1) >> 1;
@@ -901,7 +955,51 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                 else
                     hi = mid - 1;
             }
-            const Cand c = load_cand(half + (size_t)lo * RR + 1 + (i - roff[lo]));
+            return half + (size_t)lo * RR + 1 + (i - roff[lo]);
+        };
+        if constexpr (kSort) {
+            // Sort the round's successors by key, then CTA c takes the sorted
+            // positions c, c + C, ...; a position that starts a key's run
+            // relaxes the run's least-g record (the first of equal g).
+            const uint64_t nmax = (uint64_t)C * H * P::kMoves;
+            const unsigned long long *sorted = team_radix_sort<P::kMoves>(
+                team, ncand, m.sort_bits, [&](uint32_t i) { return ldcg_u32(&rec(i)->slot); }, m.sort_buf,
+                m.sort_buf + nmax, m.sort_hist, ssm, &st->error);
+            const uint32_t nxt = (r3 + 1) % 3;  // claims count toward the next round's decision
+            uint32_t claimed = 0;
+            for (uint32_t q = tid; q < nshare; q += T) {
+                const uint32_t p = cta + C * q;
+                const unsigned long long v = __ldcg(sorted + p);
+                const uint32_t key = (uint32_t)(v >> 32);
+                E e;
+                e.slot = kNone;
+                if (p == 0 || (uint32_t)(__ldcg(sorted + p - 1) >> 32) != key) {
+                    uint32_t bi = (uint32_t)v;
+                    Cand best = load_cand(rec(bi < ncand ? bi : 0));
+                    for (uint32_t p2 = p + 1; p2 < ncand; ++p2) {
+                        const unsigned long long v2 = __ldcg(sorted + p2);
+                        if ((uint32_t)(v2 >> 32) != key) break;
+                        const uint32_t i2 = (uint32_t)v2;
+                        const Cand c2 = load_cand(rec(i2 < ncand ? i2 : 0));
+                        if (P::cost_cmp(c2.g, best.g) < 0) best = c2;
+                    }
+                    uint32_t nslot = 0;
+                    const int r = relax<P>(m.tab, m.mask, m.max_probe, key, best.g, best.parent, &nslot);
+                    if (r == RELAX_FULL) {
+                        set_error(&st->err[nxt], ST_HASH_FULL);
+                    } else {
+                        claimed += (r & RELAX_CLAIMED) ? 1u : 0u;
+                        if (r & RELAX_IMPROVED) e = prob.make_entry(best.f, best.g, nslot, best.aux);
+                    }
+                }
+                stage[q] = e;
+            }
+            if (claimed) atomicAdd(s_ins2, claimed);
+            __syncthreads();
+            if (tid == 0 && *s_ins2) atomicAdd(&st->ins[nxt], (unsigned long long)*s_ins2);
+        }
+        for (uint32_t q = tid; q < (kSort ? 0u : nshare); q += T) {
+            const Cand c = load_cand(rec(cta + C * q));
             E e = prob.make_entry(c.f, c.g, c.slot, c.aux);
             if constexpr (!P::kPrevInKey) {
                 if (P::slot_g(m.tab + c.slot) == c.g)

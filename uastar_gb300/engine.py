@@ -202,10 +202,11 @@ class Engine:
 
     def __init__(self, ordinal: int = 0, *, heaps: int = 0, block_threads: int = 0, heap_capacity: int = 0,
                  hash_log2_slots: int = 0, max_load: float = 0.0, max_rounds: int = 0,
-                 wait_timeout_s: float = 0.0, threads_per_heap: int = 0, heap_top_levels: int = 0):
+                 wait_timeout_s: float = 0.0, threads_per_heap: int = 0, heap_top_levels: int = 0,
+                 dedup: int = 0):
         self._lib = L.load()
         cfg = L.Config(heaps, block_threads, heap_capacity, hash_log2_slots, max_load, max_rounds,
-                       wait_timeout_s, threads_per_heap, heap_top_levels)
+                       wait_timeout_s, threads_per_heap, heap_top_levels, dedup)
         self._h = self._lib.uastar_create(ordinal, C.byref(cfg))
         if not self._h:
             raise EngineError(L.CUDA_ERROR, f"cannot create an engine on CUDA device {ordinal}")
@@ -274,6 +275,16 @@ class Engine:
             raise EngineError(-n, "no grid solution")
         out = np.zeros(n, dtype=np.int32)
         self._lib.uastar_grid_path(self._h, _i32p(out), n)
+        return out
+
+    def sort_keys(self, keys, key_bits: int = 0) -> np.ndarray:
+        """Stable argsort of 32-bit keys by the sorted dedup mode's device
+        radix sort (uastar_sort_keys)."""
+        k = np.ascontiguousarray(np.asarray(keys, dtype=np.uint32))
+        out = np.zeros(k.size, dtype=np.uint32)
+        u32p = C.POINTER(C.c_uint32)
+        self._check(self._lib.uastar_sort_keys(self._h, k.ctypes.data_as(u32p), k.size, key_bits,
+                                               out.ctypes.data_as(u32p)), "sort_keys")
         return out
 
     # puzzle
