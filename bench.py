@@ -1,7 +1,7 @@
 """Benchmark of the GA* engine on one GB300 (or N replicas).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--sections c3,c4,c5 | --headline-only]
+                    [--sections c3,c4,c5,mb,dedup | --headline-only]
 
 Headline (one JSON line on rank 0): expanded nodes/s of the plain engine on
 the 20000 x 20000 grid (4e8 cells, 30 % blocked, corner to corner, k = 8192
@@ -11,8 +11,9 @@ re-validation).  `e2e` is the same metric through the C-ABI call that takes a
 pinned host bitmap (H2D copy, search, path D2H inside the timed region).
 The line also carries the 15-puzzle x 100 solves/s (plain engine), the mixed
 1024-instance batch solves/s (batched persistent engine) against the plain
-engine on the same mix, and the serving stream's solves/s with p50/p99
-latency.  All inputs are seeded synthetic instances (uastar_gb300.workloads).
+engine on the same mix, the serving stream's solves/s with p50/p99
+latency, the memory-bounded mode's lengths and lower bounds, and the two
+grid dedup modes (table minimum vs per-round sort + unique).  All inputs are seeded synthetic instances (uastar_gb300.workloads).
 
 --impl reference times the reference's CPU A* (the oracle restatement of
 src/pathway/CPU-solver.cpp, built from oracle/) on this host's cores: every
@@ -384,6 +385,29 @@ def section_mb(eng, args):
     return out
 
 
+def section_dedup(eng, args):
+    """The two ways of removing a round's duplicate grid successors on the
+    1000^2 and 20000^2 queries: the dedup table's atomic minimum (default)
+    and the reference's order, a device radix sort of the round's successors
+    by cell + one relax per cell (dedup = 1)."""
+    from uastar_gb300 import Engine, workloads as WL
+    out = []
+    for name, sp, log2 in (("grid_1000", WL.GRID_1000, 22), ("grid_20000", WL.GRID_20000, 28)):
+        words = sp.words()
+        for mode in (0, 1):
+            with Engine(0, heaps=8192, block_threads=256, threads_per_heap=4, hash_log2_slots=log2,
+                        dedup=mode) as e:
+                e.grid_load(words, sp.H, sp.W)
+                e.grid_solve_loaded(sp.start, sp.goal)  # warm-up
+                r = e.grid_solve_loaded(sp.start, sp.goal)
+            out.append({"workload": name, "dedup": ["table_min", "sort_unique"][mode], "ok": r.ok,
+                        "straight": r.straight, "diagonal": r.diagonal, "kernel_ms": round(r.kernel_ms, 2),
+                        "rounds": r.rounds, "us_per_round": round(1e3 * r.kernel_ms / max(1, r.rounds), 2),
+                        "expanded": r.expanded, "generated": r.generated,
+                        "expanded_per_s": round(r.expanded / (r.kernel_ms / 1e3), 1)})
+    return out
+
+
 # ------------------------------------------------------------ reference arm
 def run_reference(args, rank, world):
     if rank != 0:
@@ -429,7 +453,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--headline-only", action="store_true")
-    ap.add_argument("--sections", default="c3,c4,c5,mb")
+    ap.add_argument("--sections", default="c3,c4,c5,mb,dedup")
     ap.add_argument("--cpu-cap", type=int, default=12_000_000)
     ap.add_argument("--ref-cap", type=int, default=3_000_000)
     ap.add_argument("--c3-count", type=int, default=100)
@@ -470,12 +494,13 @@ def main():
             from uastar_gb300 import Engine
             with Engine(local_rank) as deng:
                 secs = [s for s in args.sections.split(",") if s]
-                for name, fn in [("c3", section_c3), ("c4", section_c4), ("c5", section_c5), ("mb", section_mb)]:
+                for name, fn in [("c3", section_c3), ("c4", section_c4), ("c5", section_c5), ("mb", section_mb),
+                                 ("dedup", section_dedup)]:
                     if name in secs:
                         t0 = time.perf_counter()
                         try:
                             key = {"c3": "puzzle15_x100", "c4": "mixed_1024_batched", "c5": "serving",
-                                   "mb": "memory_bounded_puzzle"}[name]
+                                   "mb": "memory_bounded_puzzle", "dedup": "dedup_modes"}[name]
                             line[key] = fn(deng, args)
                         except Exception as exc:  # report, keep the headline
                             line[f"{name}_error"] = repr(exc)
