@@ -63,9 +63,35 @@ struct GridProblem : NarrowSlots {
     // a grid node's aux is its own cell (carried into its heap entries)
     __device__ uint32_t start_aux() const { return (uint32_t)start_key(); }
     __device__ bool is_goal(uint64_t key) const { return key == (uint64_t)ex * W + ey; }
-    // the entry names its node's key: moves() can start before load_node()
+    // The entry names its node's key: moves() can start before load_node().
+    // On grids of at most 2^29 cells it also carries the move that reached
+    // the node (bits 29-31 of the cell word), and the expansion skips every
+    // successor that is the parent p or one of p's neighbours: one step from
+    // p costs at most sqrt2, two steps through the node at least 2, so the
+    // relax could never succeed.  (By induction along the parent chain this
+    // holds although the ancestors skipped successors too: a neighbour n of
+    // the node that is skipped was relaxed by the nearest ancestor that did
+    // not skip it, at that ancestor's g + one step, while the node's g is at
+    // least that g + 1 and the step from the node at least 1.)  The start
+    // node has no incoming move.  Entries that are stale are not expanded, so
+    // the move is always that of the node's current g and parent.
     static constexpr bool kEntryKey = true;
-    __device__ static uint64_t entry_key(const GridEntry &e) { return e.cell; }
+    static constexpr uint32_t kCellBits = 29;
+    __device__ __forceinline__ bool dirs() const { return (uint64_t)(uint32_t)H * (uint32_t)W <= (1ull << kCellBits); }
+    __device__ __forceinline__ uint64_t entry_key(const GridEntry &e) const {
+        return dirs() ? (e.cell & ((1u << kCellBits) - 1u)) : e.cell;
+    }
+    // successors of the move that reached a node that can never improve
+    // (bit j = move j), indexed by that move
+    __device__ __forceinline__ static uint32_t pruned(uint32_t in) {
+        return (uint32_t)(0x1529468a57ab3dceull >> (8 * in)) & 0xffu;
+    }
+    __device__ __forceinline__ uint32_t entry_moves(const GridEntry &e) const {
+        const uint64_t key = entry_key(e);
+        uint32_t m = moves(key, 0);
+        if (dirs() && key != start_key()) m &= ~pruned(e.cell >> kCellBits);
+        return m;
+    }
 
     // Octile heuristic (src/pathway/CPU-solver.cpp:139-146): with dx, dy the
     // distances to the goal, h = min(dx,dy)*sqrt2 + |dx-dy| — as a pair.
@@ -112,7 +138,7 @@ struct GridProblem : NarrowSlots {
         const int x = (int)(c / (uint32_t)W), y = (int)(c - (uint32_t)x * (uint32_t)W);
         nkey = (uint64_t)(x + c_dx(mv)) * W + (uint64_t)(y + c_dy(mv));
         ng = g + (mv < 4 ? (1ull << 32) : 1ull);
-        naux = (uint32_t)nkey;
+        naux = in_aux(nkey, mv);
         nf = ng + h_of(nkey);
     }
     // Successor in two steps (the puzzle's second step waits on a database
@@ -125,9 +151,13 @@ struct GridProblem : NarrowSlots {
         uint32_t naux;
         apply(key, g, aux, mv, s.key, s.g, naux, s.f);
     }
-    __device__ __forceinline__ void succ_end(const Succ &s, uint32_t, int, uint32_t &naux, uint64_t &nf) const {
-        naux = (uint32_t)s.key;
+    __device__ __forceinline__ void succ_end(const Succ &s, uint32_t, int mv, uint32_t &naux, uint64_t &nf) const {
+        naux = in_aux(s.key, mv);
         nf = s.f;
+    }
+    // a successor's entry cell word: its cell and, where it fits, the move
+    __device__ __forceinline__ uint32_t in_aux(uint64_t nkey, int mv) const {
+        return (uint32_t)nkey | (dirs() ? (uint32_t)mv << kCellBits : 0u);
     }
     __device__ __forceinline__ Entry make_entry(uint64_t f, uint64_t, uint32_t slot, uint32_t aux) const {
         Entry e;
@@ -339,7 +369,6 @@ template <int N> struct PuzzleProblem : NarrowSlots {
         nf = s.g + hsum(naux);
     }
     static constexpr bool kEntryKey = false;
-    __device__ static uint64_t entry_key(const PuzzleEntry &) { return 0; }
     __device__ __forceinline__ Entry make_entry(uint64_t f, uint64_t g, uint32_t slot, uint32_t) const {
         Entry e;
         e.key = ((uint32_t)f << 16) | (0xffffu - (uint32_t)g);
@@ -503,7 +532,6 @@ template <> struct PuzzleProblem<5> : WideSlots {
         nf = s.g + hsum(naux);
     }
     static constexpr bool kEntryKey = false;
-    __device__ static uint64_t entry_key(const PuzzleEntry &) { return 0; }
     __device__ __forceinline__ Entry make_entry(uint64_t f, uint64_t g, uint32_t slot, uint32_t) const {
         Entry e;
         e.key = ((uint32_t)f << 16) | (0xffffu - (uint32_t)g);

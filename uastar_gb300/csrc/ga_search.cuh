@@ -712,7 +712,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                 // where the entry names its node (grids), the neighbourhood
                 // reads start now, beside the node record's
                 uint32_t mv_pre = 0;
-                if constexpr (P::kEntryKey) mv_pre = prob.moves(P::entry_key(e), 0);
+                if constexpr (P::kEntryKey) mv_pre = prob.entry_moves(e);
                 const uint64_t fcur = prob.f_of(key, g, aux);
                 if (fcur != ecost) {
                     // stale: the node was improved after this entry was pushed
