@@ -21,11 +21,12 @@
 //            far <= the round's minimum popped f (the GA* optimality test of
 //            the reference, src/pathway/GPU-solver.cu:219-243), fail when
 //            nothing was popped.
-//   phase 2  CTA c takes candidates c, c + C, c + 2C, ... of the round's n;
-//            its threads check them in parallel (a candidate is the slot's
-//            winner iff the slot's g still equals its g; only the winner
-//            writes prev/aux) and its heap owners push the winners, dealt
-//            round-robin over the CTA's heaps.
+//   phase 2  CTA c takes the candidates of CTA (c + round) mod C's region
+//            (the successors of that CTA's pops); its threads check them in
+//            parallel (a candidate is the slot's winner iff the slot's g
+//            still equals its g; only the winner writes prev/aux) and its
+//            heap owners push the winners, dealt round-robin over the CTA's
+//            heaps.
 //
 // There is no barrier after phase 2: a CTA that finishes its pushes starts
 // the next round at once.  Its own heaps are all it pops; a relax of round
@@ -884,10 +885,13 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         // Every value read here was written before the barrier above and is
         // not written again before every CTA has read it (see TeamState), so
         // all threads decide alike.
-        // the push phase's region counts, read beside the decision's words
+        // the push phase's region counts, read beside the decision's words:
+        // the one region this CTA takes, or (kSort) every region
+        const uint32_t src = (uint32_t)((cta + round) % C);
         const uint32_t per = (C + T - 1) / T, rb = tid * per, re = min(rb + per, C);
-        const uint32_t pre0 = rb < re ? ldcg_u32(&half[(size_t)rb * RR].slot) : 0u;
-        const uint32_t pre1 = rb + 1 < re ? ldcg_u32(&half[(size_t)(rb + 1) * RR].slot) : 0u;
+        const uint32_t pre0 = kSort ? (rb < re ? ldcg_u32(&half[(size_t)rb * RR].slot) : 0u)
+                                    : ldcg_u32(&half[(size_t)src * RR].slot);
+        const uint32_t pre1 = kSort && rb + 1 < re ? ldcg_u32(&half[(size_t)(rb + 1) * RR].slot) : 0u;
         const uint64_t rmin = team.rd64(&st->round_min[r3]);
         const uint64_t gmin = team.rd64(&st->goal_min[r3]);
         if (P::cost_cmp(gmin, gbest) < 0) gbest = gmin;
@@ -922,42 +926,44 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
             st->ins[a] = 0;
             st->err[a] = 0;
         }
-        // This CTA's share of the round's candidates is every C-th one (a
-        // contiguous chunk would hold the successors of a few warps' pops,
-        // i.e. one small region of the search, and starve the rest of the
-        // team's heaps of it).  All threads check a part of the share: a
-        // candidate is the slot's winner iff the slot's g still equals its g;
-        // winners write prev/aux and are staged for their heap's owner.
-        // The round's candidates are numbered region by region: offsets of the
-        // C regions (each thread sums `per` consecutive regions' counts).
-        uint32_t mine = 0;
-        for (uint32_t r = rb; r < re; ++r) {
-            const uint32_t n = r == rb ? pre0 : r == rb + 1 ? pre1 : ldcg_u32(&half[(size_t)r * RR].slot);
-            roff[r] = n;
-            mine += n;
-        }
-        uint32_t ncand;
-        uint32_t off = block_excl_scan(mine, scratch, &ncand);
-        for (uint32_t r = rb; r < re; ++r) {
-            const uint32_t n = roff[r];
-            roff[r] = off;
-            off += n;
-        }
-        __syncthreads();
-        const uint32_t nshare = ncand > cta ? (ncand - cta + C - 1) / C : 0u;
-        // the region record of the round's candidate number i
-        const auto rec = [&](uint32_t i) -> const Cand * {
-            uint32_t lo = 0, hi = C - 1;  // the last region starting at or before i
-            while (lo < hi) {
-                const uint32_t mid = (lo + hi + 1) >> 1;
-                if (roff[mid] <= i)
-                    lo = mid;
-                else
-                    hi = mid - 1;
-            }
-            return half + (size_t)lo * RR + 1 + (i - roff[lo]);
-        };
+        // This CTA's share of the round's candidates is the whole region of
+        // CTA (c + round) mod C: the successors of that CTA's H pops, a
+        // sample of the whole search (each CTA pops its own heaps' best), read
+        // contiguously; the pairing rotates every round.  All threads check a
+        // part of the share: a candidate is the slot's winner iff the slot's
+        // g still equals its g; winners write prev/aux and are staged for
+        // their heap's owner.
+        uint32_t nshare = pre0;
         if constexpr (kSort) {
+            // The round's candidates are numbered region by region: offsets of
+            // the C regions (each thread sums `per` consecutive regions' counts).
+            uint32_t mine = 0;
+            for (uint32_t r = rb; r < re; ++r) {
+                const uint32_t n = r == rb ? pre0 : r == rb + 1 ? pre1 : ldcg_u32(&half[(size_t)r * RR].slot);
+                roff[r] = n;
+                mine += n;
+            }
+            uint32_t ncand;
+            uint32_t off = block_excl_scan(mine, scratch, &ncand);
+            for (uint32_t r = rb; r < re; ++r) {
+                const uint32_t n = roff[r];
+                roff[r] = off;
+                off += n;
+            }
+            __syncthreads();
+            nshare = ncand > cta ? (ncand - cta + C - 1) / C : 0u;
+            // the region record of the round's candidate number i
+            const auto rec = [&](uint32_t i) -> const Cand * {
+                uint32_t lo = 0, hi = C - 1;  // the last region starting at or before i
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi + 1) >> 1;
+                    if (roff[mid] <= i)
+                        lo = mid;
+                    else
+                        hi = mid - 1;
+                }
+                return half + (size_t)lo * RR + 1 + (i - roff[lo]);
+            };
             // Sort the round's successors by key, then CTA c takes the sorted
             // positions c, c + C, ...; a position that starts a key's run
             // relaxes the run's least-g record (the first of equal g).
@@ -998,8 +1004,9 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
             __syncthreads();
             if (tid == 0 && *s_ins2) atomicAdd(&st->ins[nxt], (unsigned long long)*s_ins2);
         }
+        const Cand *const sreg = half + (size_t)src * RR + 1;
         for (uint32_t q = tid; q < (kSort ? 0u : nshare); q += T) {
-            const Cand c = load_cand(rec(cta + C * q));
+            const Cand c = load_cand(sreg + q);
             E e = prob.make_entry(c.f, c.g, c.slot, c.aux);
             if constexpr (!P::kPrevInKey) {
                 if (P::slot_g(m.tab + c.slot) == c.g)
