@@ -6,6 +6,7 @@
     python -m uastar_gb300.cases mixed_small [--repeat 1]
     python -m uastar_gb300.cases cluster_small [--repeat 1]
     python -m uastar_gb300.cases pdb4 [--repeat 1]
+    python -m uastar_gb300.cases sort [--repeat 3]
 
 Each repeat solves the case once and prints one line of results; profilers
 capture the second launch of the search kernel (`-s 1 -c 1`).
@@ -21,7 +22,8 @@ from . import workloads as WL
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["grid_1000", "grid_20000", "puzzle15", "mixed_small", "cluster_small", "pdb4"])
+    ap.add_argument("case", choices=["grid_1000", "grid_20000", "puzzle15", "mixed_small", "cluster_small", "pdb4",
+                                     "sort"])
     ap.add_argument("--repeat", type=int, default=2)
     ap.add_argument("--count", type=int, default=10)
     ap.add_argument("--dedup", type=int, default=0, help="grids: 0 table minimum, 1 per-round sort + unique")
@@ -44,6 +46,19 @@ def main() -> None:
                 t0 = time.perf_counter()
                 steps = [eng.puzzle_solve(4, s.tiles()).steps for s in WL.puzzle15_x100(count=args.count)]
                 print(f"puzzle15: {len(steps)} solves in {time.perf_counter() - t0:.3f} s, steps {steps}", flush=True)
+    elif args.case == "sort":
+        # the sorted dedup mode's team sort on its own: the largest launch
+        # (2048 keys per SM) of 29-bit keys, the 20000^2 grid's cell width
+        import numpy as np
+        import torch
+        n = 2048 * torch.cuda.get_device_properties(0).multi_processor_count
+        keys = np.random.default_rng(1).integers(0, 1 << 29, n, dtype=np.uint64).astype(np.uint32)
+        with Engine(0) as eng:
+            for _ in range(args.repeat):
+                t0 = time.perf_counter()
+                perm = eng.sort_keys(keys, 29)
+                ok = bool((keys[perm][1:] >= keys[perm][:-1]).all())
+                print(f"sort: {n} keys, sorted {ok}, {1e3 * (time.perf_counter() - t0):.2f} ms with copies", flush=True)
     elif args.case == "pdb4":
         with Engine(0) as eng:
             for _ in range(args.repeat):
