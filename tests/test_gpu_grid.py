@@ -145,3 +145,23 @@ def test_problem_api_pathway(tmp_path):
     assert solve_problem(p)
     assert (tmp_path / "solutionGPU.txt").exists()
     assert abs(p.gpuOptimal - 8.243) < 1e-3
+
+
+def test_grid_beyond_2_29_cells():
+    """Grids above 2^29 cells carry no incoming move in their entries (all 8
+    moves are expanded); cell ids above 2^29 must survive the entry round
+    trip.  An open 24000^2 grid (576 M cells): on an open grid the optimum
+    from (x0, y0) to (x1, y1) is min(dx, dy) diagonal + |dx - dy| straight."""
+    H = W = 24000
+    words = np.full((H * W + 63) // 64, np.uint64(0xFFFFFFFFFFFFFFFF), dtype=np.uint64)
+    with Engine(0) as eng:
+        eng.grid_load(words, H, W)
+        for (s, g) in [((23990, 23950), (23999, 23999)), ((30, 40), (12, 3)), ((23999, 0), (23950, 7))]:
+            r = eng.grid_solve_loaded(s, g)
+            dx, dy = abs(s[0] - g[0]), abs(s[1] - g[1])
+            assert r.ok and (r.straight, r.diagonal) == (abs(dx - dy), min(dx, dy)), (s, g)
+            path = eng.grid_path()
+            a, b, _ = E.validate_grid_path(words, H, W, s, g, path)
+            assert (a, b) == (r.straight, r.diagonal)
+            if s[0] * W > (1 << 29):
+                assert int(path.min()) > (1 << 29)  # every cell id above 2^29
