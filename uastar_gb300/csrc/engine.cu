@@ -263,11 +263,22 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
     const size_t smem_budget = (size_t)std::max(8 * 1024, std::min(smem_optin, smem_sm / std::max(1, per_sm) - 2048));
     const uint32_t L = fit_levels<P>(H, c.heap_top_levels, smem_budget - sort_extra);
     const size_t smem = sorted ? SearchSmem<P>::bytes_sorted(H, L, block) : SearchSmem<P>::bytes(H, L);
-    cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return fail_cuda(eng, e, "smem attribute");
+    cudaError_t e = cudaSuccess;
+    if (eng->smem_limit[kfn] < smem) {
+        e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return fail_cuda(eng, e, "smem attribute");
+        eng->smem_limit[kfn] = smem;
+    }
     int max_active = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_active, kfn, (int)block, smem);
-    if (e != cudaSuccess) return fail_cuda(eng, e, "occupancy");
+    const auto occ_key = std::make_tuple(kfn, block, smem);
+    const auto occ = eng->occupancy.find(occ_key);
+    if (occ != eng->occupancy.end()) {
+        max_active = occ->second;
+    } else {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_active, kfn, (int)block, smem);
+        if (e != cudaSuccess) return fail_cuda(eng, e, "occupancy");
+        eng->occupancy[occ_key] = max_active;
+    }
     if (nblocks + 1 > 32 * H) {  // the push phase keeps nblocks + 1 region offsets in shared memory
         eng->set_err("too many CTAs for the heaps per CTA (need CTAs < 32 * block_threads / threads_per_heap)");
         return UASTAR_BAD_INPUT;
@@ -366,6 +377,7 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
         if (out->st.status == ST_RUNNING) break;  // paused at the cap
 
         const uint32_t s = out->st.status;
+        if (s != ST_HASH_FULL && s != ST_HEAP_OVERFLOW) break;
         size_t free_b = 0, total_b = 0;
         cudaMemGetInfo(&free_b, &total_b);
         if (s == ST_HASH_FULL && auto_table && log2 < 31 && (max_log2 <= 0 || log2 + 2 <= max_log2) &&
@@ -394,6 +406,22 @@ int32_t walk_keys(uastar_engine *eng, uint32_t goal_slot, uint64_t cap, std::vec
     eng->launches++;
     if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(eng, e, "walk launch");
     unsigned long long len = 0;
+    if (cap <= 8192) {
+        // short walks (puzzles): the whole buffer and its length in one copy
+        std::vector<uint64_t> all(cap + 1);
+        if ((e = cudaMemcpyAsync(all.data(), d_keys, (cap + 1) * 8, cudaMemcpyDeviceToHost, eng->stream)) !=
+                cudaSuccess ||
+            (e = cudaStreamSynchronize(eng->stream)) != cudaSuccess)
+            return fail_cuda(eng, e, "walk");
+        len = all[cap];
+        if (len > cap) {
+            eng->set_err("solution path longer than the walk buffer");
+            return UASTAR_ARENA_FULL;
+        }
+        keys->assign(all.begin(), all.begin() + (ptrdiff_t)len);
+        std::reverse(keys->begin(), keys->end());
+        return UASTAR_OK;
+    }
     if ((e = cudaMemcpyAsync(&len, d_len, 8, cudaMemcpyDeviceToHost, eng->stream)) != cudaSuccess)
         return fail_cuda(eng, e, "walk length");
     if ((e = cudaStreamSynchronize(eng->stream)) != cudaSuccess) return fail_cuda(eng, e, "walk");

@@ -13,6 +13,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "../../include/uastar_gpu.h"
@@ -58,6 +59,11 @@ struct uastar_engine {
     uastar::DevBuf tab, heaps, heap_size, cand, team, walk, bitmap;
     uastar::DevBuf tab_next, grow_map;  // table growth of a paused search
     uastar::DevBuf sortb;               // per-round successor sort (dedup = 1), uastar_sort_keys
+    // launch-configuration queries of the plain engine, made once per shape:
+    // the dynamic shared memory limit set per kernel, and co-resident CTAs
+    // per SM per (kernel, block, shared memory)
+    std::map<const void *, size_t> smem_limit;
+    std::map<std::tuple<const void *, uint32_t, size_t>, int> occupancy;
     int32_t gH = 0, gW = 0;
     bool grid_loaded = false;
     // pattern databases, indexed by board side
