@@ -1,0 +1,90 @@
+"""The C++ host classes (include/uastar_solvers.hpp) with the reference's
+solver names, driven through tests/cpp/solve_custom.cpp the way the
+reference's Pathway / Puzzle drive GPUPathwaySolver / GPUPuzzleSolver<N>:
+grids in the reference's custom input format, results checked like the
+reference's own output() (exact step counts, float_equal cost, valid path)."""
+from __future__ import annotations
+
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from uastar_gb300 import engine as E
+from uastar_gb300 import workloads as WL
+from uastar_gb300.problem import float_equal
+
+ROOT = Path(__file__).resolve().parents[1]
+LIB_DIR = ROOT / "uastar_gb300"
+
+
+def build_driver(out_dir: Path) -> Path:
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not on PATH")
+    if not (LIB_DIR / "libuastar_gb300.so").exists():
+        pytest.skip("engine library not built")
+    exe = out_dir / "solve_custom"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"),
+                    str(ROOT / "tests" / "cpp" / "solve_custom.cpp"), "-o", str(exe), "-L", str(LIB_DIR),
+                    "-luastar_gb300", f"-Wl,-rpath,{LIB_DIR}"], check=True)
+    return exe
+
+
+def test_host_classes_compile_against_the_abi(tmp_path):
+    assert build_driver(tmp_path).exists()
+
+
+def grid_cells(c) -> np.ndarray:
+    if c["kind"] == "custom":
+        return np.array(c["cells"], dtype=np.uint8).reshape(-1)
+    if c["kind"] == "zigzag":
+        words = E.gen_zigzag(c["H"], c["W"], c["height_gap"])[0]
+    else:
+        words = WL.GridSpec(c["H"], c["W"], c["rate"], c["seed"]).words()
+    bits = (words[:, None] >> np.arange(64, dtype=np.uint64)) & np.uint64(1)
+    return bits.reshape(-1)[: c["H"] * c["W"]].astype(np.uint8)
+
+
+@pytest.mark.gpu
+def test_host_classes_solve_like_the_reference(tmp_path):
+    exe = build_driver(tmp_path)
+    grids = golden("grid_small.json") + [golden("grid_c1.json")]
+    puzzles = [(3, r["tiles"], r["ref"]["steps"]) for r in golden("puzzle3_small.json")]
+    puzzles += [(4, r["tiles"], r["ref"]["steps"]) for r in golden("puzzle4_small.json")[:3]]
+    puzzles.append((3, [2, 1, 3, 4, 5, 6, 7, 8, 0], None))  # odd permutation: unsolvable
+    text = []
+    for c in grids:
+        cells = grid_cells(c)
+        text.append(f"pathway {c['H']} {c['W']}\n{c['start'][0]} {c['start'][1]}\n{c['goal'][0]} {c['goal'][1]}\n")
+        text.append(" ".join(map(str, cells.tolist())) + "\n")
+    for n, tiles, _ in puzzles:
+        text.append(f"puzzle {n}\n" + " ".join(map(str, tiles)) + "\n")
+    out = subprocess.run([str(exe)], input="".join(text), capture_output=True, text=True, timeout=600, check=True)
+    lines = out.stdout.strip().splitlines()
+    assert len(lines) == len(grids) + len(puzzles), out.stdout[-2000:] + out.stderr[-2000:]
+    for c, line in zip(grids, lines):
+        f = line.split()
+        assert f[0] == "pathway", line[:200]
+        ref = c["ref"]
+        assert (f[1] == "solved") == ref["solved"], (c["name"], line[:200])
+        if not ref["solved"]:
+            continue
+        cost, n = float(f[2]), int(f[3])
+        path = np.array([int(x) for x in f[4:]], dtype=np.int32)
+        assert len(path) == n
+        words = E.pack_words(grid_cells(c).reshape(c["H"], c["W"]))
+        a, b, _ = E.validate_grid_path(words, c["H"], c["W"], tuple(c["start"]), tuple(c["goal"]), path)
+        assert (a, b) == (ref["straight"], ref["diagonal"]), c["name"]
+        assert float_equal(cost, ref["cost"]), (c["name"], cost, ref["cost"])
+    for (n, tiles, steps), line in zip(puzzles, lines[len(grids):]):
+        f = line.split()
+        assert f[0] == "puzzle", line
+        if steps is None:
+            assert f[1] == "unsolved"
+            continue
+        assert f[1] == "solved" and int(f[2]) == steps, (tiles, line)
+        moves = [int(x) for x in f[4:]]
+        assert len(moves) == int(f[3]) == steps and E.validate_puzzle_moves(n, tiles, moves)
