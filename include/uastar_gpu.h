@@ -167,7 +167,9 @@ int32_t uastar_pdb_build(uastar_engine *eng, int32_t n, double *build_ms);
 int64_t uastar_pdb_bytes(int32_t n);
 /* Upload tables from the host in the reference's concatenated layout (table
  * t at the sum of the sizes of tables < t, GPU-solver.cuh:130-138) — e.g. the
- * reference's database_<n>_<tiles>.bin cache files one after the other. */
+ * reference's database_<n>_<tiles>.bin cache files one after the other.
+ * UASTAR_BAD_INPUT for a wrong size, or (n = 5) an entry above 127, the
+ * largest value the 5x5 search carries per table (the reference's largest is 39). */
 int32_t uastar_pdb_load(uastar_engine *eng, int32_t n, const uint8_t *tables, int64_t bytes);
 /* Copy the resident tables back (for the on-disk cache and byte checks). */
 int32_t uastar_pdb_fetch(uastar_engine *eng, int32_t n, uint8_t *out, int64_t bytes);

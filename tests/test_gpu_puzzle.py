@@ -189,3 +189,21 @@ def test_memory_bounded_24_puzzle(peng):
     assert 0 < r["lower_bound"] <= r["steps"]
     mv = peng.puzzle_moves()
     assert len(mv) == r["steps"] and E.validate_puzzle_moves(5, tiles, mv)
+
+
+def test_pdb5_load_checks_the_field_width(peng):
+    """Loaded 5x5 tables (the reference's cache files) work like built ones;
+    an entry above the 7 bits the search keeps per table is refused, and the
+    engine then holds no 5x5 tables."""
+    t = peng.pdb_fetch(5)
+    row = golden("puzzle5_small.json")[0]
+    with Engine(0) as e2:
+        e2.pdb_load(5, t)
+        r = e2.puzzle_solve(5, row["tiles"])
+        assert r.ok and r.steps == row["ref"]["steps"]
+        bad = t.copy()
+        bad[123457] = 200
+        with pytest.raises(EngineError):
+            e2.pdb_load(5, bad)
+        with pytest.raises(EngineError):
+            e2.puzzle_solve(5, row["tiles"])

@@ -163,7 +163,7 @@ int32_t check_max(uastar_engine *eng, const uint8_t *t, uint64_t n, uint32_t lim
     if ((e = cudaStreamSynchronize(eng->stream)) != cudaSuccess) return fail_cuda(eng, e, "pdb check");
     if (mx > limit) {
         eng->set_err("pattern database entry above the search's field width");
-        return UASTAR_CUDA_ERROR;
+        return UASTAR_BAD_INPUT;
     }
     return UASTAR_OK;
 }
@@ -276,6 +276,10 @@ int32_t uastar_pdb_load(uastar_engine *eng, int32_t n, const uint8_t *tables, in
         cudaSuccess)
         return fail_cuda(eng, e, "pdb upload");
     if ((e = cudaStreamSynchronize(eng->stream)) != cudaSuccess) return fail_cuda(eng, e, "pdb upload");
+    eng->pdb_ready[n] = false;
+    // the 5x5 search keeps each table's value in 7 bits of the node record
+    if (n == 5)
+        if (int32_t rc = check_max(eng, eng->pdb[n].as<uint8_t>(), (uint64_t)need, 127)) return rc;
     eng->pdb_ready[n] = true;
     return UASTAR_OK;
 }
