@@ -363,26 +363,6 @@ inline int log2_u64(uint64_t v) {
     while ((1ull << l) < v) ++l;
     return l;
 }
-uint64_t pack_board(int n, const uint8_t *tiles) {
-    uint64_t k = 0;
-    for (int i = 0; i < n * n; ++i) k |= (uint64_t)(tiles[i] & 15) << (4 * i);
-    return k;
-}
-bool board_solvable(int n, const uint8_t *tiles) {
-    int inv = 0, brow = 0, seen = 0;
-    for (int i = 0; i < n * n; ++i) {
-        if (tiles[i] >= n * n || (seen >> tiles[i] & 1)) return false;
-        seen |= 1 << tiles[i];
-        if (!tiles[i]) {
-            brow = i / n;
-            continue;
-        }
-        for (int j = i + 1; j < n * n; ++j)
-            if (tiles[j] && tiles[j] < tiles[i]) ++inv;
-    }
-    if (n & 1) return (inv & 1) == 0;
-    return ((inv + brow) & 1) == ((n - 1) & 1);
-}
 
 // Estimated dedup nodes of an instance (a sizing hint; overflow is retried).
 uint64_t est_nodes(const uastar_instance &in) {

@@ -574,12 +574,6 @@ int32_t grid_solve_impl(uastar_engine *eng, const uint64_t *host_words, int32_t 
     return out->status;
 }
 
-uint64_t pack_board(int n, const uint8_t *tiles) {
-    uint64_t k = 0;
-    for (int i = 0; i < n * n; ++i) k |= (uint64_t)(tiles[i] & 15) << (4 * i);
-    return k;
-}
-
 bool board_ok(int n, const uint8_t *tiles) {
     int seen = 0;
     for (int i = 0; i < n * n; ++i) {
@@ -587,24 +581,6 @@ bool board_ok(int n, const uint8_t *tiles) {
         seen |= 1 << tiles[i];
     }
     return true;
-}
-
-// Solvability: the goal has no inversions and the blank in row n-1.  A
-// horizontal move keeps the inversion parity; a vertical move changes it by
-// n-1 and moves the blank one row.  So a board is solvable iff inversions are
-// even (n odd), or inversions + blank row has the parity of n-1 (n even).
-bool board_solvable(int n, const uint8_t *tiles) {
-    int inv = 0, brow = 0;
-    for (int i = 0; i < n * n; ++i) {
-        if (!tiles[i]) {
-            brow = i / n;
-            continue;
-        }
-        for (int j = i + 1; j < n * n; ++j)
-            if (tiles[j] && tiles[j] < tiles[i]) ++inv;
-    }
-    if (n & 1) return (inv & 1) == 0;
-    return ((inv + brow) & 1) == ((n - 1) & 1);
 }
 
 template <int N>

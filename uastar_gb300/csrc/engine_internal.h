@@ -41,6 +41,32 @@ struct DevBuf {
     template <class T> T *as() const { return static_cast<T *>(p); }
 };
 
+// A 3x3 / 4x4 board packed as the search's 64-bit key (cell c in bits 4c..4c+3).
+inline uint64_t pack_board(int n, const uint8_t *tiles) {
+    uint64_t k = 0;
+    for (int i = 0; i < n * n; ++i) k |= (uint64_t)(tiles[i] & 15) << (4 * i);
+    return k;
+}
+
+// Solvability of a valid board: the goal has no inversions and the blank in
+// row n-1.  A horizontal move keeps the inversion parity; a vertical move
+// changes it by n-1 and moves the blank one row.  So a board is solvable iff
+// inversions are even (n odd), or inversions + blank row has the parity of
+// n-1 (n even).
+inline bool board_solvable(int n, const uint8_t *tiles) {
+    int inv = 0, brow = 0;
+    for (int i = 0; i < n * n; ++i) {
+        if (!tiles[i]) {
+            brow = i / n;
+            continue;
+        }
+        for (int j = i + 1; j < n * n; ++j)
+            if (tiles[j] && tiles[j] < tiles[i]) ++inv;
+    }
+    if (n & 1) return (inv & 1) == 0;
+    return ((inv + brow) & 1) == ((n - 1) & 1);
+}
+
 struct ServeState;  // batch.cu
 
 }  // namespace uastar
