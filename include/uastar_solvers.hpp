@@ -21,9 +21,11 @@
 #pragma once
 
 #include <cstdint>
+#include <cstdio>
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "uastar_gpu.h"
@@ -57,6 +59,25 @@ public:
 private:
     uastar_engine *eng_;
 };
+// The reference's disjoint patterns, in its tracked order
+// (src/puzzle/CPU-solver.hpp:43-102), and its cache file names
+// (src/puzzle/database.cpp:86-91).
+inline std::vector<std::vector<int>> partitions(int n) {
+    if (n == 3) return {{1, 2, 3, 4, 5, 6, 7, 8}};
+    if (n == 4) return {{1, 2, 3, 4, 5, 6, 9, 13}, {7, 8, 10, 11, 12, 14, 15}};
+    return {{3, 4, 5, 10, 15, 20}, {2, 1, 6, 11, 16, 21}, {7, 8, 9, 12, 17, 22}, {13, 14, 18, 19, 23, 24}};
+}
+inline std::string cache_name(int n, const std::vector<int> &tiles) {
+    std::string s = "database_" + std::to_string(n);
+    for (int t : tiles) s += "_" + std::to_string(t);
+    return s + ".bin";
+}
+// Entries of a table over k tracked tiles: (n*n)! / (n*n - k)!.
+inline size_t table_bytes(int n, size_t k) {
+    size_t b = 1;
+    for (size_t i = 0; i < k; ++i) b *= (size_t)(n * n) - i;
+    return b;
+}
 }  // namespace detail
 
 template <class PathwayT>
@@ -118,23 +139,72 @@ class GPUPuzzleSolver {
     static_assert(N >= 3 && N <= 5, "3x3, 4x4 or 5x5 boards");
 
 public:
-    explicit GPUPuzzleSolver(PuzzleT *puzzle, int ordinal = 0, const uastar_config *cfg = nullptr)
-        : p_(puzzle), ordinal_(ordinal), has_cfg_(cfg != nullptr) {
+    /* `cache_dir`: where the reference's database_<n>_<tiles>.bin cache files
+     * are read and written ("." = the working directory, as the reference
+     * does; "" = no files). */
+    explicit GPUPuzzleSolver(PuzzleT *puzzle, int ordinal = 0, const uastar_config *cfg = nullptr,
+                             std::string cache_dir = ".")
+        : p_(puzzle), ordinal_(ordinal), has_cfg_(cfg != nullptr), cache_dir_(std::move(cache_dir)) {
         if (cfg) cfg_ = *cfg;
     }
 
     /* GPU-solver.cuh:64-195: device setup and the disjoint pattern databases,
-     * built on the GPU — or, when `tables` holds the bytes of the reference's
-     * database_<n>_<tiles>.bin files concatenated in its order, loaded. */
-    void initialize(const std::vector<uint8_t> *tables = nullptr) {
+     * the way the reference's fetchDatabase treats its cache
+     * (database.cpp:86-122): with every table's file present they are read
+     * (a short file throws, where the reference exits); otherwise the tables
+     * are built on the GPU and the missing files written. */
+    void initialize() {
         eng_.reset(new detail::Engine(ordinal_, has_cfg_ ? &cfg_ : nullptr));
-        if (tables) {
-            eng_->check(uastar_pdb_load(eng_->get(), N, tables->data(), (int64_t)tables->size()), "database load");
-        } else {
-            double ms = 0;
-            eng_->check(uastar_pdb_build(eng_->get(), N, &ms), "database build");
+        const std::vector<std::vector<int>> parts = detail::partitions(N);
+        std::vector<std::string> paths;
+        bool all = !cache_dir_.empty();
+        for (const auto &t : parts) {
+            paths.push_back(cache_dir_ + "/" + detail::cache_name(N, t));
+            if (all) {
+                std::FILE *f = std::fopen(paths.back().c_str(), "rb");
+                all = f != nullptr;
+                if (f) std::fclose(f);
+            }
+        }
+        const size_t total = (size_t)uastar_pdb_bytes(N);
+        if (all) {
+            std::vector<uint8_t> tables(total);
+            size_t off = 0;
+            for (size_t i = 0; i < parts.size(); ++i) {
+                const size_t bytes = detail::table_bytes(N, parts[i].size());
+                std::FILE *f = std::fopen(paths[i].c_str(), "rb");
+                const size_t got = f ? std::fread(tables.data() + off, 1, bytes, f) : 0;
+                if (f) std::fclose(f);
+                if (got != bytes) throw SolverError(UASTAR_BAD_INPUT, paths[i] + " is not intact");
+                off += bytes;
+            }
+            eng_->check(uastar_pdb_load(eng_->get(), N, tables.data(), (int64_t)total), "database load");
+            source_ = "cache";
+            return;
+        }
+        double ms = 0;
+        eng_->check(uastar_pdb_build(eng_->get(), N, &ms), "database build");
+        source_ = "gpu";
+        if (cache_dir_.empty()) return;
+        std::vector<uint8_t> tables(total);
+        eng_->check(uastar_pdb_fetch(eng_->get(), N, tables.data(), (int64_t)total), "database fetch");
+        size_t off = 0;
+        for (size_t i = 0; i < parts.size(); ++i) {
+            const size_t bytes = detail::table_bytes(N, parts[i].size());
+            std::FILE *f = std::fopen(paths[i].c_str(), "rb");
+            if (f) {
+                std::fclose(f);  // present: the reference keeps its own file
+            } else if (!(f = std::fopen(paths[i].c_str(), "wb")) ||
+                       std::fwrite(tables.data() + off, 1, bytes, f) != bytes || std::fclose(f) != 0) {
+                std::remove(paths[i].c_str());
+                throw SolverError(UASTAR_BAD_INPUT, paths[i] + " cannot be written");
+            }
+            off += bytes;
         }
     }
+
+    /* Where initialize() took the tables from: "cache" or "gpu". */
+    const char *databaseSource() const { return source_; }
 
     /* GPU-solver.cuh:197-274: true iff the board is solvable (the reference
      * would search forever on an unsolvable one). */
@@ -166,6 +236,8 @@ private:
     PuzzleT *p_;
     int ordinal_;
     bool has_cfg_;
+    std::string cache_dir_;
+    const char *source_ = "";
     uastar_config cfg_{};
     std::unique_ptr<detail::Engine> eng_;
     uastar_puzzle_result res_{};

@@ -11,6 +11,9 @@
 //   <n*n ints, 0 = blank>
 // For each problem one line: "pathway solved <cost> <n> <ids...>" or
 // "puzzle solved <steps> <n> <moves...>", "... unsolved", or "error <status>".
+// argv[1]: the pattern-database cache directory ("." when absent, as in the
+// reference; "" for none); where each puzzle's tables came from goes to
+// stderr as "database cache|gpu".
 #include <cstdio>
 #include <iostream>
 #include <string>
@@ -40,9 +43,10 @@ struct Puzzle {
 };
 
 template <int N>
-void solve_puzzle(Puzzle &pz) {
-    uastar_host::GPUPuzzleSolver<N, Puzzle> solver(&pz);
+void solve_puzzle(Puzzle &pz, const std::string &cache_dir) {
+    uastar_host::GPUPuzzleSolver<N, Puzzle> solver(&pz, 0, nullptr, cache_dir);
     solver.initialize();
+    std::fprintf(stderr, "database %s\n", solver.databaseSource());
     if (!solver.solve()) {
         std::printf("puzzle unsolved\n");
         return;
@@ -57,7 +61,8 @@ void solve_puzzle(Puzzle &pz) {
 
 }  // namespace
 
-int main() {
+int main(int argc, char **argv) {
+    const std::string cache_dir = argc > 1 ? argv[1] : ".";
     std::string kind;
     while (std::cin >> kind) {
         try {
@@ -93,11 +98,11 @@ int main() {
                     t = (uint8_t)v;
                 }
                 if (n == 3)
-                    solve_puzzle<3>(pz);
+                    solve_puzzle<3>(pz, cache_dir);
                 else if (n == 4)
-                    solve_puzzle<4>(pz);
+                    solve_puzzle<4>(pz, cache_dir);
                 else
-                    solve_puzzle<5>(pz);
+                    solve_puzzle<5>(pz, cache_dir);
             } else {
                 std::printf("error %d\n", (int)UASTAR_BAD_INPUT);
                 return 2;

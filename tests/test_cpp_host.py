@@ -62,7 +62,8 @@ def test_host_classes_solve_like_the_reference(tmp_path):
         text.append(" ".join(map(str, cells.tolist())) + "\n")
     for n, tiles, _ in puzzles:
         text.append(f"puzzle {n}\n" + " ".join(map(str, tiles)) + "\n")
-    out = subprocess.run([str(exe)], input="".join(text), capture_output=True, text=True, timeout=600, check=True)
+    out = subprocess.run([str(exe), ""], input="".join(text), capture_output=True, text=True, timeout=600,
+                         check=True)
     lines = out.stdout.strip().splitlines()
     assert len(lines) == len(grids) + len(puzzles), out.stdout[-2000:] + out.stderr[-2000:]
     for c, line in zip(grids, lines):
@@ -88,3 +89,30 @@ def test_host_classes_solve_like_the_reference(tmp_path):
         assert f[1] == "solved" and int(f[2]) == steps, (tiles, line)
         moves = [int(x) for x in f[4:]]
         assert len(moves) == int(f[3]) == steps and E.validate_puzzle_moves(n, tiles, moves)
+
+
+@pytest.mark.gpu
+def test_puzzle_solver_keeps_the_reference_cache_files(tmp_path):
+    """GPUPuzzleSolver::initialize treats database_<n>_<tiles>.bin like the
+    reference's fetchDatabase: without the file the tables are built (on the
+    GPU) and written — byte-identical to the reference's own file — and the
+    next solver reads them; a short file is refused."""
+    import hashlib
+
+    exe = build_driver(tmp_path)
+    cache = tmp_path / "cache"
+    cache.mkdir()
+    rows = golden("puzzle3_small.json")[:2]
+    text = "".join(f"puzzle 3\n{' '.join(map(str, r['tiles']))}\n" for r in rows)
+    out = subprocess.run([str(exe), str(cache)], input=text, capture_output=True, text=True, timeout=300,
+                         check=True)
+    assert out.stderr.split() == ["database", "gpu", "database", "cache"], out.stderr
+    for r, line in zip(rows, out.stdout.strip().splitlines()):
+        assert line.split()[:3] == ["puzzle", "solved", str(r["ref"]["steps"])]
+    name = "database_3_1_2_3_4_5_6_7_8.bin"
+    data = (cache / name).read_bytes()
+    assert hashlib.sha256(data).hexdigest() == golden("pdb_sha256.json")[name]["sha256"]
+    (cache / name).write_bytes(data[:1000])
+    out = subprocess.run([str(exe), str(cache)], input="".join(text.splitlines(keepends=True)[:2]),
+                         capture_output=True, text=True, timeout=300, check=True)
+    assert out.stdout.startswith("error") and "not intact" in out.stdout
