@@ -104,19 +104,19 @@ public:
     /* GPU-solver.cu:180-328: true iff a path from (sx, sy) to (ex, ey) exists. */
     bool solve() {
         res_ = uastar_grid_result{};
-        const int32_t rc = uastar_grid_solve_loaded(eng_->get(), p_->sx(), p_->sy(), p_->ex(), p_->ey(), &res_);
+        const int32_t rc = uastar_grid_solve_loaded(engine().get(), p_->sx(), p_->sy(), p_->ex(), p_->ey(), &res_);
         if (rc == UASTAR_NO_SOLUTION) return false;
-        eng_->check(rc, "grid solve");
+        engine().check(rc, "grid solve");
         return true;
     }
 
     /* GPU-solver.cu:330-354: the float32 cost along the path (as the
      * reference accumulates it) and the cell ids start -> goal. */
     void getSolution(float *optimal, std::vector<int> *pathList) {
-        const int64_t n = uastar_grid_path(eng_->get(), nullptr, 0);
+        const int64_t n = uastar_grid_path(engine().get(), nullptr, 0);
         if (n < 0) throw SolverError((int32_t)-n, "no grid solution to read");
         pathList->resize((size_t)n);
-        uastar_grid_path(eng_->get(), reinterpret_cast<int32_t *>(pathList->data()), n);
+        uastar_grid_path(engine().get(), reinterpret_cast<int32_t *>(pathList->data()), n);
         *optimal = res_.cost;
     }
 
@@ -126,6 +126,10 @@ public:
 
 private:
     static_assert(sizeof(int) == sizeof(int32_t), "path ids are written as int32");
+    detail::Engine &engine() const {
+        if (!eng_) throw SolverError(UASTAR_BAD_INPUT, "initialize() has not run");
+        return *eng_;
+    }
     PathwayT *p_;
     int ordinal_;
     bool has_cfg_;
@@ -214,25 +218,29 @@ public:
         if (tiles.size() != (size_t)(N * N))
             throw SolverError(UASTAR_BAD_INPUT, "initial state must hold N*N tiles");
         res_ = uastar_puzzle_result{};
-        const int32_t rc = uastar_puzzle_solve(eng_->get(), N, tiles.data(), &res_);
+        const int32_t rc = uastar_puzzle_solve(engine().get(), N, tiles.data(), &res_);
         if (rc == UASTAR_NO_SOLUTION) return false;
-        eng_->check(rc, "puzzle solve");
+        engine().check(rc, "puzzle solve");
         return true;
     }
 
     /* GPU-solver.cuh:276-287: the optimal move count and the moves start ->
      * goal, each 0..3 indexing the reference's DX/DY (GPU-kernel.cuh:494-495). */
     void getSolution(int *optimal, std::vector<int> *pathList) {
-        const int64_t n = uastar_puzzle_moves(eng_->get(), nullptr, 0);
+        const int64_t n = uastar_puzzle_moves(engine().get(), nullptr, 0);
         if (n < 0) throw SolverError((int32_t)-n, "no puzzle solution to read");
         pathList->resize((size_t)n);
-        uastar_puzzle_moves(eng_->get(), reinterpret_cast<int32_t *>(pathList->data()), n);
+        uastar_puzzle_moves(engine().get(), reinterpret_cast<int32_t *>(pathList->data()), n);
         *optimal = res_.steps;
     }
 
     const uastar_puzzle_result &result() const { return res_; }
 
 private:
+    detail::Engine &engine() const {
+        if (!eng_) throw SolverError(UASTAR_BAD_INPUT, "initialize() has not run");
+        return *eng_;
+    }
     PuzzleT *p_;
     int ordinal_;
     bool has_cfg_;

@@ -116,3 +116,39 @@ def test_puzzle_solver_keeps_the_reference_cache_files(tmp_path):
     out = subprocess.run([str(exe), str(cache)], input="".join(text.splitlines(keepends=True)[:2]),
                          capture_output=True, text=True, timeout=300, check=True)
     assert out.stdout.startswith("error") and "not intact" in out.stdout
+
+
+def test_calls_before_initialize_throw(tmp_path):
+    """solve() / getSolution() before initialize() throw SolverError
+    (UASTAR_BAD_INPUT) instead of touching a missing engine; no GPU needed."""
+    if shutil.which("g++") is None or not (LIB_DIR / "libuastar_gb300.so").exists():
+        pytest.skip("g++ or the engine library missing")
+    src = tmp_path / "early.cpp"
+    src.write_text(r"""
+#include <cstdio>
+#include <vector>
+#include "uastar_solvers.hpp"
+struct Pathway {
+    std::vector<uint8_t> g{1};
+    int sx() const { return 0; } int sy() const { return 0; } int ex() const { return 0; }
+    int ey() const { return 0; } int width() const { return 1; } int height() const { return 1; }
+    const uint8_t *graph() const { return g.data(); }
+};
+struct Puzzle { void initialState(std::vector<uint8_t> &d) { d.assign(9, 0); } };
+int main() {
+    Pathway p; Puzzle z;
+    uastar_host::GPUPathwaySolver<Pathway> a(&p);
+    uastar_host::GPUPuzzleSolver<3, Puzzle> b(&z);
+    int caught = 0;
+    try { a.solve(); } catch (const uastar_host::SolverError &e) { caught += e.status() == UASTAR_BAD_INPUT; }
+    try { float c; std::vector<int> v; a.getSolution(&c, &v); } catch (const uastar_host::SolverError &e) { caught += e.status() == UASTAR_BAD_INPUT; }
+    try { b.solve(); } catch (const uastar_host::SolverError &e) { caught += e.status() == UASTAR_BAD_INPUT; }
+    std::printf("%d\n", caught);
+    return caught == 3 ? 0 : 1;
+}
+""")
+    exe = tmp_path / "early"
+    subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"), str(src), "-o",
+                    str(exe), "-L", str(LIB_DIR), "-luastar_gb300", f"-Wl,-rpath,{LIB_DIR}"], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0 and out.stdout.strip() == "3", out.stdout + out.stderr
