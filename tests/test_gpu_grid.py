@@ -1,6 +1,6 @@
 """GPU grid engine (plain, whole-GPU team) against the reference's results.
 
-Parity bar (the benchmark spec's): the same number of straight and diagonal
+Parity bar: the same number of straight and diagonal
 steps as the reference's CPU A*, its float32 cost within the reference's own
 tolerance (float_equal: 1e-3 absolute or 200 ULPs, src/utils.hpp:86-111), and
 a path that re-validates on the host."""
