@@ -60,7 +60,7 @@ typedef struct {
     int32_t heaps;           /* k parallel binary heaps of the plain engine (0 -> 8192 grid, 16384 puzzle) */
     int32_t block_threads;   /* CTA size of the plain engine's persistent kernel (0 -> 256) */
     int32_t heap_capacity;   /* entries per heap (0 -> auto, grown on overflow) */
-    int32_t hash_log2_slots; /* dedup table = 2^n slots of 32 B (0 -> sized from the instance and
+    int32_t hash_log2_slots; /* dedup table = 2^n slots of 32 B, n <= 31 (0 -> sized from the instance and
                               grown 4x in place whenever it is half full) */
     double max_load;         /* dedup table load limit in (0,1) (0 -> 0.8) */
     int64_t max_rounds;      /* GA* round limit per solve (0 -> 2^31) */
@@ -113,7 +113,8 @@ typedef struct {
 } uastar_grid_result;
 
 /* Upload a grid bitmap and keep it resident (replaces the graph H2D copy,
- * GPU-solver.cu:140).  words holds ceil(H*W/64) words. */
+ * GPU-solver.cu:140).  words holds ceil(H*W/64) words; H*W < 2^31 (path
+ * cell ids are int32, like the reference's vector<int>). */
 int32_t uastar_grid_load(uastar_engine *eng, const uint64_t *words, int32_t H, int32_t W);
 /* Solve on the resident grid (replaces GPUPathwaySolver::solve, GPU-solver.cu:180-328,
  * plus its kInitialize seeding, GPU-kernel.cuh:141-164). */

@@ -385,7 +385,7 @@ struct BatchPlan {
 
 int32_t check_instance(const uastar_instance &in) {
     if (in.kind == UASTAR_KIND_GRID) {
-        if (!in.words || in.H <= 0 || in.W <= 0 || (uint64_t)in.H * in.W >= (1ull << 32)) return UASTAR_BAD_INPUT;
+        if (!in.words || in.H <= 0 || in.W <= 0 || (uint64_t)in.H * in.W >= (1ull << 31)) return UASTAR_BAD_INPUT;
         if (in.sx < 0 || in.sx >= in.H || in.sy < 0 || in.sy >= in.W || in.ex < 0 || in.ex >= in.H ||
             in.ey < 0 || in.ey >= in.W)
             return UASTAR_BAD_INPUT;
@@ -1339,7 +1339,7 @@ static void serve_grow(ServeState *S, ServeTier &t, int q) {
     InstDesc &d = t.descs[q];
     const uint64_t old_n = 1ull << d.log2_slots, new_n = old_n * 4;
     uint64_t noff = 0;
-    if (new_n > (1ull << 32) || !S->tab_alloc.alloc(new_n, 4, &noff)) {
+    if (new_n > (1ull << 31) || !S->tab_alloc.alloc(new_n, 4, &noff)) {
         d.grow_at = 0;
         return;
     }

@@ -206,7 +206,8 @@ bool grow_table(uastar_engine *eng, SearchMem<typename P::Entry> &m, uint32_t k,
     cudaMemGetInfo(&free_b, &total_b);
     const size_t need = (new_n * sizeof(Slot) > eng->tab_next.bytes ? new_n * sizeof(Slot) : 0) +
                         (old_n * 4 > eng->grow_map.bytes ? old_n * 4 : 0);
-    if (new_n > (1ull << 32) || need + (256ull << 20) > free_b) return false;
+    // at most 2^31 slots: every slot index stays below the no-parent mark kNone
+    if (new_n > (1ull << 31) || need + (256ull << 20) > free_b) return false;
     if (eng->tab_next.ensure(new_n * sizeof(Slot)) != cudaSuccess) return false;
     if (eng->grow_map.ensure(old_n * 4) != cudaSuccess) return false;
     if (fill_ff(eng, eng->tab_next.p, new_n * sizeof(Slot)) != UASTAR_OK) return false;
@@ -239,6 +240,10 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
     const uint32_t nblocks = (plain_heaps<P>(c) + H - 1) / H;
     const uint32_t k = nblocks * H;
     int log2 = c.hash_log2_slots > 0 ? c.hash_log2_slots : log2_auto;
+    if (log2 > 31) {
+        eng->set_err("hash_log2_slots must be at most 31");
+        return UASTAR_BAD_INPUT;
+    }
     if (max_log2 > 0) log2 = std::min(log2, max_log2);
     uint32_t stride = c.heap_capacity > 0 ? next_pow2_u32((uint32_t)c.heap_capacity + 1) : stride_auto;
     if (c.dedup != 0 && c.dedup != 1) {
@@ -380,7 +385,7 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
         if (s != ST_HASH_FULL && s != ST_HEAP_OVERFLOW) break;
         size_t free_b = 0, total_b = 0;
         cudaMemGetInfo(&free_b, &total_b);
-        if (s == ST_HASH_FULL && auto_table && log2 < 31 && (max_log2 <= 0 || log2 + 2 <= max_log2) &&
+        if (s == ST_HASH_FULL && auto_table && log2 + 2 <= 31 && (max_log2 <= 0 || log2 + 2 <= max_log2) &&
             (out->slots * 4 * sizeof(Slot)) < free_b + eng->tab.bytes) {
             log2 += 2;
             continue;
@@ -466,8 +471,8 @@ int32_t walk_keys_wide(uastar_engine *eng, uint32_t goal_slot, uint64_t cap, std
 
 int32_t grid_load_impl(uastar_engine *eng, const uint64_t *words, int32_t H, int32_t W) {
     if (!eng) return UASTAR_BAD_INPUT;
-    if (!words || H <= 0 || W <= 0 || (uint64_t)H * (uint64_t)W >= (1ull << 32)) {
-        eng->set_err("grid must be non-empty with H*W < 2^32 cells");
+    if (!words || H <= 0 || W <= 0 || (uint64_t)H * (uint64_t)W >= (1ull << 31)) {
+        eng->set_err("grid must be non-empty with H*W < 2^31 cells (path cell ids are int32, as in the reference)");
         return UASTAR_BAD_INPUT;
     }
     const uint64_t cells = (uint64_t)H * W;
