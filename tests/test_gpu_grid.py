@@ -97,8 +97,9 @@ def test_bad_inputs(engine):
         engine.grid_solve(w, 4, 4, (0, 0), (4, 4))
     with pytest.raises(EngineError):
         engine.grid_solve(w, 0, 4, (0, 0), (0, 0))
+    big = np.zeros(E.grid_words(46341, 46341), dtype=np.uint64)  # untouched pages
     with pytest.raises(EngineError):  # 2^31 cells or more: path ids would not fit int32
-        engine.grid_solve(w, 46341, 46341, (0, 0), (1, 1))
+        engine.grid_solve(big, 46341, 46341, (0, 0), (1, 1))
     with Engine(0, hash_log2_slots=32) as eng:  # above the 2^31-slot table limit
         with pytest.raises(EngineError):
             eng.grid_solve(w, 4, 4, (0, 0), (3, 3))

@@ -100,3 +100,18 @@ def test_validate_puzzle_moves():
     assert not E.validate_puzzle_moves(3, t, [3])
     assert not E.validate_puzzle_moves(3, t, [0])  # off the board
     assert not E.validate_puzzle_moves(3, [1, 1, 3, 4, 5, 6, 7, 0, 8], [2])  # not a permutation
+
+
+def test_short_bitmaps_are_refused_before_the_c_side():
+    """The C functions read ceil(H*W/64) words from the pointer they get; the
+    Python wrappers check the array covers the grid first."""
+    short = np.zeros(3, dtype=np.uint64)  # 192 cells
+    with pytest.raises(ValueError):
+        E.grid_reachable(short, 20, 20, (0, 0), (19, 19))
+    with pytest.raises(ValueError):
+        E.grid_screen(short, 20, 20, (0, 0), (19, 19))
+    with pytest.raises(ValueError):
+        E.validate_grid_path(short, 20, 20, (0, 0), (19, 19), [0, 21])
+    # a list of Python ints is converted, not misread
+    words = E.pack_words(np.ones((8, 8), dtype=np.uint8))
+    assert E.grid_reachable([int(x) for x in words], 8, 8, (0, 0), (7, 7))

@@ -36,6 +36,15 @@ def grid_words(H: int, W: int) -> int:
     return (H * W + 63) // 64
 
 
+def _bitmap(words, H: int, W: int) -> np.ndarray:
+    """The bitmap as contiguous uint64 words, checked to cover H x W cells:
+    the C side reads ceil(H*W/64) words from the pointer it is given."""
+    w = np.ascontiguousarray(words, dtype=np.uint64)
+    if H > 0 and W > 0 and w.size < grid_words(H, W):
+        raise ValueError(f"bitmap of {w.size} words is short of the {grid_words(H, W)} a {H}x{W} grid needs")
+    return w
+
+
 # ------------------------------------------------------------ host utilities
 def gen_grid(seed: int, H: int, W: int, block_rate: float, start=(0, 0), goal=None) -> np.ndarray:
     """Seeded Bernoulli grid bitmap (1 = open) with start and goal forced open."""
@@ -72,13 +81,15 @@ def gen_zigzag(H: int, W: int, height_gap: int):
 
 def grid_reachable(words: np.ndarray, H: int, W: int, start, goal) -> bool:
     lib = L.load()
-    return bool(lib.uastar_grid_reachable(_u64p(words), H, W, start[0], start[1], goal[0], goal[1]))
+    w = _bitmap(words, H, W)
+    return bool(lib.uastar_grid_reachable(_u64p(w), H, W, start[0], start[1], goal[0], goal[1]))
 
 
 def grid_screen(words: np.ndarray, H: int, W: int, start, goal, limit: int = 200_000) -> int:
     """1 = reachable, 0 = unreachable (proven), 2 = presumed reachable (both sides large)."""
     lib = L.load()
-    return int(lib.uastar_grid_screen(_u64p(words), H, W, start[0], start[1], goal[0], goal[1], limit))
+    w = _bitmap(words, H, W)
+    return int(lib.uastar_grid_screen(_u64p(w), H, W, start[0], start[1], goal[0], goal[1], limit))
 
 
 def validate_grid_path(words: np.ndarray, H: int, W: int, start, goal, path: Sequence[int]):
@@ -86,7 +97,8 @@ def validate_grid_path(words: np.ndarray, H: int, W: int, start, goal, path: Seq
     lib = L.load()
     p = np.ascontiguousarray(np.asarray(path, dtype=np.int32))
     a, b, c = C.c_int64(), C.c_int64(), C.c_float()
-    rc = lib.uastar_validate_grid_path(_u64p(words), H, W, start[0], start[1], goal[0], goal[1], _i32p(p),
+    w = _bitmap(words, H, W)
+    rc = lib.uastar_validate_grid_path(_u64p(w), H, W, start[0], start[1], goal[0], goal[1], _i32p(p),
                                        len(p), C.byref(a), C.byref(b), C.byref(c))
     if rc:
         raise EngineError(rc, "grid path failed validation")
@@ -176,7 +188,7 @@ class PuzzleInstance:
 def _to_struct(inst, keep: list) -> L.Instance:
     s = L.Instance()
     if isinstance(inst, GridInstance):
-        w = np.ascontiguousarray(inst.words, dtype=np.uint64)
+        w = _bitmap(inst.words, inst.H, inst.W)
         keep.append(w)
         s.kind = L.KIND_GRID
         s.H, s.W = inst.H, inst.W
@@ -246,7 +258,7 @@ class Engine:
 
     # grid
     def grid_load(self, words: np.ndarray, H: int, W: int) -> None:
-        w = np.ascontiguousarray(words, dtype=np.uint64)
+        w = _bitmap(words, H, W)
         self._check(self._lib.uastar_grid_load(self._h, _u64p(w), H, W), "grid_load")
 
     def _grid_sol(self, r: L.GridResult) -> GridSolution:
@@ -262,7 +274,7 @@ class Engine:
         return self._grid_sol(r)
 
     def grid_solve(self, words: np.ndarray, H: int, W: int, start, goal) -> GridSolution:
-        w = np.ascontiguousarray(words, dtype=np.uint64)
+        w = _bitmap(words, H, W)
         r = L.GridResult()
         self._lib.uastar_grid_solve(self._h, _u64p(w), H, W, start[0], start[1], goal[0], goal[1], C.byref(r))
         if r.status in (L.CUDA_ERROR, L.BAD_INPUT, L.TIMEOUT):
