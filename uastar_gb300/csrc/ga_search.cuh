@@ -43,9 +43,11 @@
 // This replaces the reference's per-round kExtractExpand -> host copy ->
 // MergesortPairs -> kAssign -> host copy -> kDeduplicate -> kHeapInsert
 // chain (src/pathway/GPU-solver.cu:180-328) with one persistent kernel and
-// no host round trip: the per-round sort + unique of the successor list is
-// replaced by the table's atomic minimum (same result: the minimum g per
-// state among this round's successors and the stored node).
+// no host round trip: by default the per-round sort + unique of the
+// successor list is replaced by the table's atomic minimum (same result: the
+// minimum g per state among this round's successors and the stored node);
+// the kSort variant keeps the reference's order with a team radix sort
+// (ga_sort.cuh) between the decision and the push phase.
 #pragma once
 #include <cstdint>
 
