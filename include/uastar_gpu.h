@@ -92,6 +92,15 @@ int64_t uastar_kernel_launches(const uastar_engine *eng);
 /* Name of this library build (architecture it was compiled for). */
 const char *uastar_build_info(void);
 
+/* Measurement aid (no counterpart in the reference): the latency floor of one
+ * round of the plain engine's persistent kernel on its launch geometry (the
+ * engine's heaps, block_threads and threads_per_heap).  us_barrier: rounds
+ * of one team barrier only; us_cas_barrier: rounds of one 16-byte atomicCAS
+ * per thread on a pseudo-random slot of a dedup table larger than L2 (values
+ * left as they are; each thread's next slot depends on the CAS's result)
+ * followed by the barrier.  Runs `rounds` (1 .. 2^20) rounds of each. */
+int32_t uastar_round_floor(uastar_engine *eng, int32_t rounds, double *us_barrier, double *us_cas_barrier);
+
 /* ---- grid pathfinding (--pathway) ------------------------------------- */
 typedef struct {
     int32_t status;
@@ -276,8 +285,15 @@ typedef struct {
 int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int32_t count,
                            const uastar_batch_config *cfg, uastar_instance_result *results,
                            uastar_batch_stats *stats);
-/* Pick threads_per_instance / heap_capacity / load_factor for a workload by
- * timing candidate configurations on a sample of it.  Writes the choice. */
+/* Pick the batch geometry for a workload by timing configurations on a
+ * sample of it: one pass of coordinate descent from the defaults over
+ * threads_per_instance {128, 256, 512}, threads_per_heap {2, 4, 8} (heaps per
+ * instance = their quotient), heap_capacity {1023, 4095, 16383},
+ * load_factor {0.35, 0.5, 0.7}, cluster_size {4, 8, 16} and tier1_rounds
+ * {1024, 2048, 4096}, each knob taking the value of least wall time with
+ * the others held.  Writes the choice; best->reserved = configurations timed.
+ * Replaces the reference's compile-time sizes (src/pathway/GPU-solver.hpp:6-17,
+ * src/puzzle/GPU-solver.cuh:11-20). */
 int32_t uastar_autotune(uastar_engine *eng, const uastar_instance *sample, int32_t count,
                         uastar_batch_config *best);
 
@@ -342,8 +358,13 @@ double uastar_now_s(void);
  * cells are rejected with UASTAR_BAD_INPUT; a search that outgrows the array
  * (2^20 dedup slots at 80 % load, 256 heaps of 4095 entries) reports
  * UASTAR_HASH_FULL or UASTAR_HEAP_OVERFLOW in the result, a path longer than
- * path_cap UASTAR_ARENA_FULL.  All calls share the array: calls that overlap
- * on the GPU race, so serialize them. */
+ * path_cap UASTAR_ARENA_FULL (path_len 0), and a team-barrier wait that
+ * exceeds 10 s UASTAR_TIMEOUT.  A return value other than UASTAR_OK means
+ * nothing was queued that writes the result record; an error still pending
+ * from the caller's earlier CUDA work is returned as UASTAR_CUDA_ERROR and
+ * left pending.  The array's address is looked up once per device and kept:
+ * do not call this again in a process after cudaDeviceReset.  All calls share
+ * the array: calls that overlap on the GPU race, so serialize them. */
 typedef struct {
     int32_t status;
     int32_t reserved;

@@ -58,8 +58,21 @@ def lib() -> C.CDLL:
         l.oracle_pdb_build.argtypes = [C.c_int, i32p, C.c_int, C.POINTER(C.c_uint8)]
         l.oracle_puzzle_astar.argtypes = [C.c_int, C.POINTER(C.c_uint8), C.POINTER(C.POINTER(C.c_uint8)),
                                           C.c_int64, i32p, C.c_int64, C.POINTER(PuzzleResult)]
+        l.oracle_gen_grid.argtypes = [C.c_uint64, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
+                                      C.c_int, u64p]
         _lib = l
     return _lib
+
+
+def gen_grid(seed: int, H: int, W: int, rate: float, start=(0, 0), goal=None) -> np.ndarray:
+    """The benchmarks' seeded Bernoulli grid (1 = open), built by the oracle
+    library alone (the same bits as the engine's generator)."""
+    goal = (H - 1, W - 1) if goal is None else goal
+    words = np.zeros((H * W + 63) // 64, dtype=np.uint64)
+    if lib().oracle_gen_grid(seed & (2**64 - 1), H, W, float(rate), start[0], start[1], goal[0], goal[1],
+                             words.ctypes.data_as(C.POINTER(C.c_uint64))):
+        raise ValueError("bad grid parameters")
+    return words
 
 
 def grid_astar(words: np.ndarray, H: int, W: int, start, goal, max_expansions: int = 0, want_path=True):

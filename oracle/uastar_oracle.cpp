@@ -570,4 +570,34 @@ int oracle_puzzle_astar(int n, const uint8_t *tiles, const uint8_t *const *pdbs,
     return 0;
 }
 
+// ------------------------------------------------------------- inputs ----
+// The seeded Bernoulli grid of the benchmarks, restated so that the CPU
+// timing arms can build their inputs without loading the GPU engine: cell id
+// is blocked iff the top 32 bits of splitmix64 output #id (Steele, Lea &
+// Flood, OOPSLA 2014; output #i of seed s = mix(s + (i + 1) * 0x9E3779B97F4A7C15))
+// fall below floor(rate * 2^32); start and goal are forced open; bit
+// (id & 63) of word id >> 6, 1 = open.  The reference has no random input
+// module (src/pathway/pathway.cpp:53-64 accepts custom and zigzag only).
+int oracle_gen_grid(uint64_t seed, int H, int W, double rate, int sx, int sy, int ex, int ey, uint64_t *words) {
+    if (H <= 0 || W <= 0 || !words) return 1;
+    const uint64_t cells = (uint64_t)H * (uint64_t)W, nwords = (cells + 63) / 64;
+    const double t = std::floor(rate * 4294967296.0);
+    const uint64_t thr = t >= 4294967296.0 ? (1ull << 32) : (uint64_t)t;
+    for (uint64_t w = 0; w < nwords; ++w) {
+        uint64_t v = 0;
+        for (uint64_t b = 0; b < 64 && w * 64 + b < cells; ++b) {
+            uint64_t z = seed + (w * 64 + b + 1) * 0x9E3779B97F4A7C15ull;
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+            z ^= z >> 31;
+            if ((z >> 32) >= thr) v |= 1ull << b;
+        }
+        words[w] = v;
+    }
+    const uint64_t s = (uint64_t)sx * W + sy, e = (uint64_t)ex * W + ey;
+    words[s >> 6] |= 1ull << (s & 63);
+    words[e >> 6] |= 1ull << (e & 63);
+    return 0;
+}
+
 }  // extern "C"

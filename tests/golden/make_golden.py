@@ -4,6 +4,7 @@ oracle/Makefile.ref into oracle/_ref/) on the engine's seeded instances.
 
     python tests/golden/make_golden.py small c1      # seconds
     python tests/golden/make_golden.py c3 c4 c2      # minutes (c2 needs ~10 GB RAM)
+    python tests/golden/make_golden.py c5            # ~30 min: the serving stream's 512-request sample
     python tests/golden/make_golden.py pdb           # after `ref_puzzle pdb 4` (and 5) cached the tables
     python tests/golden/make_golden.py p24small      # after `ref_puzzle pdb 5`
 
@@ -207,6 +208,44 @@ def part_c4(jobs=8):
     (GOLDEN / "mixed_c4.json").write_text(json.dumps(rows, indent=0))
 
 
+def serve_sample(stream, n_big: int = 64, n_long: int = 64, n_rest: int = 384):
+    """Indices of the serving stream's golden sample: its n_big largest grids,
+    its n_long longest puzzle walks and n_rest more in a seeded order."""
+    grids = sorted((i for i, (_, s) in enumerate(stream) if isinstance(s, WL.GridSpec)),
+                   key=lambda i: (-stream[i][1].H, i))[:n_big]
+    walks = sorted((i for i, (_, s) in enumerate(stream) if isinstance(s, WL.PuzzleSpec)),
+                   key=lambda i: (-stream[i][1].walk, i))[:n_long]
+    chosen = set(grids) | set(walks)
+    rest = sorted((i for i in range(len(stream)) if i not in chosen), key=lambda i: WL.splitmix64(0xC5C5, i))
+    return sorted(chosen | set(rest[:n_rest]))
+
+
+def part_c5(jobs=8, puzzle_jobs=4):
+    stream = WL.serve_stream(20000, 1.0)
+    idx = serve_sample(stream)
+    pz = [i for i in idx if isinstance(stream[i][1], WL.PuzzleSpec)]
+    gr = [i for i in idx if isinstance(stream[i][1], WL.GridSpec)]
+    pres = ref_puzzle_parallel(4, [stream[i][1].tiles().tolist() for i in pz], "c5p", puzzle_jobs)
+    rows = {}
+    for i, r in zip(pz, pres):
+        s = stream[i][1]
+        rows[i] = {"index": i, "kind": "puzzle", "seed": s.seed, "walk": s.walk,
+                   "ref": {k: r[k] for k in ("solved", "steps", "stored", "solve_seconds")}}
+
+    def one(i):
+        s = stream[i][1]
+        rec = grid_case(f"c5_{i}", s.words(), s.H, s.W, s.start, s.goal,
+                        {"kind": "random", "rate": s.rate, "seed": s.seed}, keep_path=False)
+        rec["kind"] = "grid"
+        rec["index"] = i
+        return rec
+
+    with cf.ThreadPoolExecutor(jobs) as ex:
+        for rec in ex.map(one, gr):
+            rows[rec["index"]] = rec
+    (GOLDEN / "serve_c5_sample.json").write_text(json.dumps([rows[i] for i in idx], indent=0))
+
+
 def part_pdb():
     out = {}
     for p in sorted(PDB_DIR.glob("database_*.bin")):
@@ -215,7 +254,7 @@ def part_pdb():
 
 
 PARTS = {"small": part_small, "p15small": part_p15small, "p24small": part_p24small, "c1": part_c1, "c2": part_c2,
-         "c3": part_c3, "c4": part_c4, "pdb": part_pdb}
+         "c3": part_c3, "c4": part_c4, "c5": part_c5, "pdb": part_pdb}
 
 if __name__ == "__main__":
     if not (REF / "ref_grid").exists():

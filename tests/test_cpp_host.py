@@ -152,3 +152,72 @@ int main() {
                     str(exe), "-L", str(LIB_DIR), "-luastar_gb300", f"-Wl,-rpath,{LIB_DIR}"], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert out.returncode == 0 and out.stdout.strip() == "3", out.stdout + out.stderr
+
+
+# ---------------------------------------------------------------------------
+# The reference's own problem classes over the binding.  Pathway
+# (src/pathway/pathway.cpp) and Puzzle (src/puzzle/puzzle.cu) are compiled
+# unmodified from the reference's source tree with tests/cpp/ref_binding/ in
+# front of the include path, so their `#include "pathway/GPU-solver.hpp"` /
+# `"puzzle/GPU-solver.cuh"` take the binding in place of the reference's
+# moderngpu solvers; tests/cpp/ref_problem_driver.cpp runs the reference's
+# solve_problem sequence (src/main.cpp:60-110) on them.  The reference tree is
+# where the golden fixtures were made; where it is absent (a GPU machine) the test
+# skips, and the GPU half of the binding is exercised by the solve_custom
+# driver above.
+def reference_tree():
+    import __graft_entry__ as G
+    return G.REFERENCE_TREE
+
+
+def build_ref_driver(out_dir: Path) -> Path:
+    ref = reference_tree()
+    if not (ref / "src" / "pathway" / "pathway.cpp").exists():
+        pytest.skip("the reference's source tree is not on this host")
+    if shutil.which("g++") is None or not (LIB_DIR / "libuastar_gb300.so").exists():
+        pytest.skip("g++ or the engine library missing")
+    exe = out_dir / "ref_problem_driver"
+    src = ref / "src"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-w", "-include", "cstring", "-include", "cstdio",
+                    "-I", str(ROOT / "tests" / "cpp" / "ref_binding"), "-I", str(ROOT / "include"),
+                    "-I", str(ROOT / "oracle" / "ref_shim"), "-I", str(src), "-I", str(ref / "libs" / "bitmap"),
+                    "-I", str(ROOT / "oracle" / "ref_harness"), str(ROOT / "tests" / "cpp" / "ref_problem_driver.cpp"),
+                    str(src / "pathway" / "pathway.cpp"), str(src / "pathway" / "CPU-solver.cpp"),
+                    str(src / "pathway" / "input" / "custom.cpp"), str(src / "pathway" / "input" / "zigzag.cpp"),
+                    str(src / "puzzle" / "database.cpp"), "-x", "c++", str(src / "puzzle" / "puzzle.cu"), "-x", "none",
+                    "-L", str(LIB_DIR), "-luastar_gb300", f"-Wl,-rpath,{LIB_DIR}", "-o", str(exe)], check=True)
+    return exe
+
+
+def gpu_present() -> bool:
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except ImportError:
+        return False
+
+
+def test_reference_problem_classes_run_over_the_binding(tmp_path):
+    exe = build_ref_driver(tmp_path)
+    c = next(x for x in golden("grid_small.json") if x["kind"] == "custom")
+    cells = np.array(c["cells"], dtype=np.uint8).reshape(c["H"], c["W"])
+    text = f"{c['start'][0]} {c['start'][1]} {c['goal'][0]} {c['goal'][1]}\n" + \
+        "\n".join(" ".join(str(int(v)) for v in row) for row in cells) + "\n"
+    run = lambda args, inp: subprocess.run([str(exe), *args], input=inp, capture_output=True, text=True,
+                                           cwd=tmp_path, timeout=300)
+    # the CPU half: the reference's own solver through its own classes
+    r = run(["pathway", str(c["H"]), str(c["W"]), "--no-gpu"], text)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert f"Optimal distance from CPU: {c['ref']['cost']:.3f}" in r.stdout
+    p3 = golden("puzzle3_small.json")[3]
+    board = " ".join(map(str, p3["tiles"])) + "\n"
+    r = run(["puzzle", "3", "--no-gpu"], board)
+    assert r.returncode == 0 and f"Optimal steps from CPU: {p3['ref']['steps']}" in r.stdout, r.stdout
+    # the whole sequence: output() compares the CPU and the GPU (binding) results
+    for args, inp in ((["pathway", str(c["H"]), str(c["W"])], text), (["puzzle", "3"], board)):
+        r = run(args, inp)
+        if gpu_present():
+            assert r.returncode == 0, r.stdout + r.stderr
+            assert "Optimal" in r.stdout and "not consistent" not in r.stdout
+        else:  # no GPU on this host: the binding reports it instead of exiting
+            assert r.returncode == 3 and "cannot create an engine" in r.stdout, r.stdout

@@ -1,0 +1,74 @@
+"""The batched and serving engines on their benchmark workloads, against the
+reference's own results: the whole 1024-instance mix (768 15-puzzles with
+walks of 60..300 moves + 256 grids of 256..4096 per side) in one batch call,
+and the serving stream's 512-request sample (its 64 largest 8192-side grids,
+its 64 longest walks and 384 more) served through the serving loop.  The
+fixtures hold the reference CPU A*'s optimal costs (tests/golden/make_golden.py
+parts c4 and c5); every path is also re-validated on the host by the engine."""
+from __future__ import annotations
+
+import time
+
+import pytest
+
+from conftest import golden
+from uastar_gb300 import Engine
+from uastar_gb300 import _lib as L
+from uastar_gb300 import workloads as WL
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def eng4():
+    with Engine(0) as eng:
+        eng.pdb_build(4)
+        yield eng
+
+
+def agrees(spec, r, ref) -> bool:
+    if r["status"] != L.OK:
+        return False
+    if isinstance(spec, WL.PuzzleSpec):
+        return r["steps"] == ref["steps"]
+    return (r["straight"], r["diagonal"]) == (ref["straight"], ref["diagonal"])
+
+
+def test_full_mixed_batch_matches_reference(eng4):
+    rows = golden("mixed_c4.json")
+    specs = WL.mixed_1024()
+    assert len(rows) == len(specs) == 1024
+    for row, s in zip(rows, specs):  # the fixture describes these very instances
+        assert row["kind"] == ("puzzle" if isinstance(s, WL.PuzzleSpec) else "grid")
+        assert row["seed"] == s.seed
+    res, st = eng4.batch_solve([s.instance() for s in specs])
+    bad = [i for i, (s, r, row) in enumerate(zip(specs, res, rows)) if not agrees(s, r, row["ref"])]
+    assert not bad, f"{len(bad)} of 1024 differ from the reference, first {bad[:5]}"
+    assert st["expanded"] > 0
+
+
+def test_serving_sample_matches_reference(eng4):
+    rows = golden("serve_c5_sample.json")
+    stream = WL.serve_stream(20000, 1.0)
+    sample = [(r["index"], r) for r in rows]
+    for i, row in sample:
+        s = stream[i][1]
+        assert row["seed"] == s.seed and row["kind"] == ("puzzle" if isinstance(s, WL.PuzzleSpec) else "grid")
+    # the whole sample arrives within a second (the tail of the largest grids
+    # keeps many requests resident together); budget as in the benchmark
+    eng4.serve_start(hbm_budget_gb=120.0)
+    t0 = WL.E.now_s() + 0.2
+    ids = {}
+    for k, (i, _row) in enumerate(sample):
+        ids[eng4.serve_submit(stream[i][1].instance(), t0 + k * 0.002)] = i
+    got = {}
+    deadline = time.time() + 600
+    while len(got) < len(ids) and time.time() < deadline:
+        for rid, r in eng4.serve_poll():
+            got[ids[rid]] = r
+        time.sleep(0.005)
+    stats = eng4.serve_stop(30.0)
+    assert len(got) == len(ids), f"{len(got)} of {len(ids)} completed"
+    assert stats["peak_resident"] > 1
+    bad = [i for i, row in sample if not agrees(stream[i][1], got[i], row["ref"])]
+    assert not bad, f"{len(bad)} of {len(sample)} served results differ from the reference, first {bad[:5]}"

@@ -115,3 +115,28 @@ def test_short_bitmaps_are_refused_before_the_c_side():
     # a list of Python ints is converted, not misread
     words = E.pack_words(np.ones((8, 8), dtype=np.uint8))
     assert E.grid_reachable([int(x) for x in words], 8, 8, (0, 0), (7, 7))
+
+
+def test_serving_stream_screen_table_matches_the_screen():
+    # the recorded screen of the 20000-request serving stream equals a fresh
+    # screen on a sample of its grids (those skipped past their first seed
+    # and others), and the stream built from it is the screened stream
+    import json
+    from pathlib import Path
+    table = json.loads((Path(WL.__file__).with_name("serve_stream_screen.json")).read_text())
+    offsets = {int(k): v for k, v in table["offsets"].items()}
+    stream = WL.serve_stream(table["count"], 1.0)
+    grids = [i for i, (_, s) in enumerate(stream) if isinstance(s, WL.GridSpec)]
+    skipped = sorted(offsets)[::max(1, len(offsets) // 12)][:12]
+    plain = [i for i in grids if i not in offsets][::max(1, len(grids) // 12)][:12]
+    for i in skipped + plain:
+        s = stream[i][1]
+        base = WL.splitmix64(0x5E57E ^ 0x99, i) & 0xFFFFFFFF
+        assert s.seed == base + offsets.get(i, 0)
+        assert WL.screened_grid(s.H, s.W, s.rate, base).seed == s.seed, i
+
+
+def test_oracle_generator_equals_engine_generator():
+    import oracle as O
+    for seed, H, W, rate in [(7, 300, 333, 0.3), (1, 1000, 1000, 0.3), (5, 17, 5, 0.9), (3, 1, 70, 0.5)]:
+        assert (O.gen_grid(seed, H, W, rate) == E.gen_grid(seed, H, W, rate)).all()

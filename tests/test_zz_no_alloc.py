@@ -86,3 +86,16 @@ def test_noalloc_rejects_oversized_grids_and_reports_unreachable():
     g[20, :] = 0
     res, path = solve_noalloc(E.pack_words(g), 40, 40, (0, 0), (39, 39), 64)
     assert res.status == L.NO_SOLUTION and res.path_len == 0
+
+
+def test_noalloc_reports_a_short_path_buffer_and_a_full_table():
+    # a solvable grid whose path is longer than the caller's buffer
+    sp = WL.screened_grid(300, 300, 0.2, 8, exact=True)
+    res, _ = solve_noalloc(sp.words(), sp.H, sp.W, sp.start, sp.goal, path_cap=50)
+    assert res.status == L.ARENA_FULL and res.path_len == 0
+    # a goal walled off from a start whose component (1500 x 2048 open
+    # cells) is larger than the fixed table's 0.8 * 2^20 slots
+    g = np.ones((2048, 2048), dtype=np.uint8)
+    g[1500, :] = 0
+    res, _ = solve_noalloc(E.pack_words(g), 2048, 2048, (0, 0), (2047, 2047), 64)
+    assert res.status == L.HASH_FULL and res.path_len == 0

@@ -115,6 +115,7 @@ SIGNATURES = [
     ("uastar_set_stream", C.c_int32, [_P, _P]),
     ("uastar_kernel_launches", C.c_int64, [_P]),
     ("uastar_build_info", C.c_char_p, []),
+    ("uastar_round_floor", C.c_int32, [_P, C.c_int32, _DP, _DP]),
     ("uastar_grid_load", C.c_int32, [_P, _U64P, C.c_int32, C.c_int32]),
     ("uastar_grid_solve_loaded", C.c_int32, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                              C.POINTER(GridResult)]),

@@ -646,12 +646,31 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
     };
     cudaEventRecord(k0, eng->stream);
     if (use_graph) {
+        // The launch is captured every call (its arguments change) and the
+        // executable graph of this launch shape, instantiated once, is
+        // updated in place; a shape seen for the first time, or an update
+        // the driver refuses, instantiates a new one.
         e = cudaStreamBeginCapture(eng->stream, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
             enqueue();
             e = cudaStreamEndCapture(eng->stream, &graph);
         }
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+        const auto key = std::make_tuple(g.csize, ctas, g.T, g.smem);
+        auto it = eng->b_graphs.find(key);
+        if (e == cudaSuccess && it != eng->b_graphs.end()) {
+            cudaGraphExecUpdateResultInfo info;
+            if (cudaGraphExecUpdate(it->second, graph, &info) == cudaSuccess) {
+                exec = it->second;
+            } else {
+                cudaGetLastError();  // the refused update is not an error of the launch
+                cudaGraphExecDestroy(it->second);
+                eng->b_graphs.erase(it);
+            }
+        }
+        if (e == cudaSuccess && !exec) {
+            e = cudaGraphInstantiate(&exec, graph, 0);
+            if (e == cudaSuccess) eng->b_graphs[key] = exec;
+        }
         if (e == cudaSuccess) e = cudaGraphLaunch(exec, eng->stream);
     } else {
         enqueue();
@@ -659,16 +678,11 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
     }
     eng->launches++;
     cudaEventRecord(k1, eng->stream);
-    if (e != cudaSuccess) {
-        if (exec) cudaGraphExecDestroy(exec);
-        if (graph) cudaGraphDestroy(graph);
-        return fail_cuda(eng, e, "batch launch");
-    }
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail_cuda(eng, e, "batch launch");
     std::vector<InstOut> outs(cnt);
     e = cudaMemcpyAsync(outs.data(), eng->b_out.p, cnt * sizeof(InstOut), cudaMemcpyDeviceToHost, eng->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(eng->stream);
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
     if (e != cudaSuccess) return fail_cuda(eng, e, "batch kernel");
     float kms = 0;
     cudaEventElapsedTime(&kms, k0, k1);
@@ -911,38 +925,69 @@ int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int
 int32_t uastar_autotune(uastar_engine *eng, const uastar_instance *sample, int32_t count,
                         uastar_batch_config *best) {
     if (!eng || !sample || count <= 0 || !best) return UASTAR_BAD_INPUT;
-    const int Ts[] = {128, 256, 512};
-    const int tphs[] = {2, 4};
-    const int caps[] = {2048};
-    const double loads[] = {0.35, 0.6};
+    // Coordinate descent over the batch geometry, one pass: starting from the
+    // defaults, each knob in turn takes the value that solves the sample in
+    // the least wall time with the others held.  Knobs: CTA size per
+    // instance, threads per heap (together: heaps per instance), entries per
+    // heap, dedup-partition load factor, CTAs per cluster team and the
+    // single-CTA tier's round budget.
+    struct Knob {
+        int32_t uastar_batch_config::*i;
+        double uastar_batch_config::*d;
+        std::vector<double> values;
+    };
+    const std::vector<Knob> knobs = {
+        {&uastar_batch_config::threads_per_instance, nullptr, {128, 256, 512}},
+        {&uastar_batch_config::threads_per_heap, nullptr, {2, 4, 8}},
+        {&uastar_batch_config::heap_capacity, nullptr, {1023, 4095, 16383}},
+        {nullptr, &uastar_batch_config::load_factor, {0.35, 0.5, 0.7}},
+        {&uastar_batch_config::cluster_size, nullptr, {4, 8, 16}},
+        {&uastar_batch_config::tier1_rounds, nullptr, {1024, 2048, 4096}},
+    };
+    uastar_batch_config cur{};
+    cur.threads_per_instance = 256;
+    cur.threads_per_heap = 4;
+    cur.heap_capacity = 4095;
+    cur.load_factor = 0.5;
+    cur.cluster_size = 8;
+    cur.tier1_rounds = 2048;
+    cur.use_graph = 1;
     std::vector<uastar_instance_result> res(count);
-    double best_ms = 1e300;
-    uastar_batch_config pick{};
-    for (int T : Ts)
-        for (int tph : tphs)
-        for (int cap : caps)
-            for (double ld : loads) {
-                uastar_batch_config c{};
-                c.threads_per_instance = T;
-                c.threads_per_heap = tph;
-                c.heap_capacity = cap;
-                c.load_factor = ld;
-                c.use_graph = 1;
-                uastar_batch_stats s;
-                if (uastar_batch_solve(eng, sample, count, &c, res.data(), &s) != UASTAR_OK) continue;
-                bool ok = true;
-                for (auto &r : res) ok &= (r.status == UASTAR_OK || r.status == UASTAR_NO_SOLUTION);
-                if (!ok) continue;
-                if (s.wall_ms < best_ms) {
-                    best_ms = s.wall_ms;
-                    pick = c;
-                }
+    auto time_of = [&](const uastar_batch_config &c) -> double {
+        uastar_batch_stats s;
+        if (uastar_batch_solve(eng, sample, count, &c, res.data(), &s) != UASTAR_OK) return 1e300;
+        for (auto &r : res)
+            if (r.status != UASTAR_OK && r.status != UASTAR_NO_SOLUTION) return 1e300;
+        return s.wall_ms;
+    };
+    double best_ms = time_of(cur);
+    int tried = 1;
+    for (const Knob &k : knobs) {
+        uastar_batch_config keep = cur;
+        for (double v : k.values) {
+            uastar_batch_config c = cur;
+            if (k.i) {
+                if (c.*k.i == (int32_t)v) continue;
+                c.*k.i = (int32_t)v;
+            } else {
+                if (c.*k.d == v) continue;
+                c.*k.d = v;
             }
+            const double ms = time_of(c);
+            ++tried;
+            if (ms < best_ms) {
+                best_ms = ms;
+                keep = c;
+            }
+        }
+        cur = keep;
+    }
     if (best_ms >= 1e300) {
         eng->set_err("autotune: no configuration solved the sample");
         return UASTAR_CUDA_ERROR;
     }
-    *best = pick;
+    *best = cur;
+    best->reserved = tried;
     return UASTAR_OK;
 }
 

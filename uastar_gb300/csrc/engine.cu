@@ -84,6 +84,28 @@ __global__ void k_best_open(PuzzleProblem<N> prob, SearchMem<PuzzleEntry> m, uin
     }
 }
 
+// Round-latency floor of the plain engine's launch geometry: `rounds` rounds
+// of one team barrier each.  With `tab` set, every thread first does one
+// 16-byte atomicCAS on a pseudo-random slot of the dedup table and the next
+// round's slot depends on what it returned (a dependent chain, like a relax
+// that waits for its CAS); compare and swap values are the same word, so
+// the table is never changed.
+__global__ void __launch_bounds__(512, 1) k_round_floor(TeamState *st, uint64_t timeout_ns, Slot *tab,
+                                                        uint64_t mask, uint32_t rounds) {
+    GridTeam team{st, 0u, timeout_ns};
+    uint64_t x = mix64((uint64_t)blockIdx.x * blockDim.x + threadIdx.x + 1);
+    const KeyG probe{0x5A5A5A5A5A5A5A5Aull, 0x5A5A5A5A5A5A5A5Aull};
+    for (uint32_t r = 0; r < rounds; ++r) {
+        if (tab) {
+            const KeyG seen = cas128(tab + (x & mask), probe, probe);
+            x = mix64(x ^ seen.key ^ r);
+        }
+        team.sync();
+        if (ldcg_u32(&st->error)) break;
+    }
+    if (x == 0) st->pad0_ = 1;  // keeps the chain live (x is never 0 in practice)
+}
+
 // Walk the prev chain from the goal slot (one thread: a pointer chase).
 // Writes keys goal -> start; *len = count, or cap + 1 when truncated.
 __global__ void k_walk(const Slot *tab, uint32_t goal_slot, unsigned long long *keys,
@@ -752,6 +774,7 @@ void uastar_destroy(uastar_engine *eng) {
                       &eng->b_walklen, &eng->b_cstate, &eng->b_cnext})
         b->release();
     for (auto &b : eng->pdb) b.release();
+    for (auto &kv : eng->b_graphs) cudaGraphExecDestroy(kv.second);
     if (eng->ev0) cudaEventDestroy(eng->ev0);
     if (eng->ev1) cudaEventDestroy(eng->ev1);
     if (eng->own_stream) cudaStreamDestroy(eng->own_stream);
@@ -811,6 +834,62 @@ int32_t uastar_sort_keys(uastar_engine *eng, const uint32_t *keys, int64_t n, in
         eng->set_err("sort: a team barrier gave up");
         return UASTAR_TIMEOUT;
     }
+    return UASTAR_OK;
+}
+
+int32_t uastar_round_floor(uastar_engine *eng, int32_t rounds, double *us_barrier, double *us_cas_barrier) {
+    if (!eng || rounds <= 0 || rounds > (1 << 20)) return UASTAR_BAD_INPUT;
+    cudaSetDevice(eng->device);
+    const uastar_config &c = eng->cfg;
+    const uint32_t block = (uint32_t)c.block_threads;
+    const uint32_t tph = c.threads_per_heap > 0 ? (uint32_t)c.threads_per_heap : 4u;
+    const uint32_t H = std::max(1u, block / std::min(tph, block));
+    const uint32_t nblocks = (plain_heaps<GridProblem>(c) + H - 1) / H;
+    int max_active = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_active, (const void *)k_round_floor,
+                                                                  (int)block, 0);
+    if (e != cudaSuccess) return fail_cuda(eng, e, "occupancy");
+    if ((uint64_t)max_active * eng->sms < nblocks) {
+        eng->set_err("round floor: the launch geometry exceeds one co-resident wave");
+        return UASTAR_BAD_INPUT;
+    }
+    // a table larger than L2, so that the CAS is a memory round trip
+    const uint64_t slots = std::max<uint64_t>(1ull << 26, eng->tab.bytes / sizeof(Slot));
+    if ((e = eng->tab.ensure(slots * sizeof(Slot))) != cudaSuccess) return fail_cuda(eng, e, "alloc table");
+    if ((e = eng->team.ensure(sizeof(TeamState))) != cudaSuccess) return fail_cuda(eng, e, "alloc state");
+    uint64_t n = 1;
+    while (n * 2 <= eng->tab.bytes / sizeof(Slot)) n *= 2;
+    TeamState *st = eng->team.as<TeamState>();
+    uint64_t timeout_ns = (uint64_t)(c.wait_timeout_s * 1e9);
+    double out[2] = {0, 0};
+    for (int mode = 0; mode < 2; ++mode) {
+        TeamState init = fresh_team_state();
+        if ((e = cudaMemcpyAsync(st, &init, sizeof init, cudaMemcpyHostToDevice, eng->stream)) != cudaSuccess)
+            return fail_cuda(eng, e, "state upload");
+        Slot *tab = mode ? eng->tab.as<Slot>() : nullptr;
+        uint64_t mask = n - 1;
+        uint32_t r = (uint32_t)rounds;
+        void *args[] = {&st, &timeout_ns, &tab, &mask, &r};
+        cudaEventRecord(eng->ev0, eng->stream);
+        e = cudaLaunchCooperativeKernel((const void *)k_round_floor, dim3(nblocks), dim3(block), args, 0,
+                                        eng->stream);
+        if (e != cudaSuccess) return fail_cuda(eng, e, "round floor launch");
+        eng->launches++;
+        cudaEventRecord(eng->ev1, eng->stream);
+        uint32_t err = 0;
+        if ((e = cudaMemcpyAsync(&err, &st->error, 4, cudaMemcpyDeviceToHost, eng->stream)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(eng->stream)) != cudaSuccess)
+            return fail_cuda(eng, e, "round floor");
+        if (err) {
+            eng->set_err("round floor: a team barrier gave up");
+            return UASTAR_TIMEOUT;
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, eng->ev0, eng->ev1);
+        out[mode] = 1e3 * ms / rounds;
+    }
+    if (us_barrier) *us_barrier = out[0];
+    if (us_cas_barrier) *us_cas_barrier = out[1];
     return UASTAR_OK;
 }
 

@@ -110,6 +110,10 @@ struct uastar_engine {
     uastar::DevBuf b_desc, b_out, b_queue, b_bitmaps, b_tab, b_heaps, b_hsize, b_cand, b_walk,
         b_walklen, b_cstate, b_cnext;
     uastar::ServeState *serve = nullptr;  // owned; released by uastar_serve_stop
+    // instantiated launch graphs of the batched engine, one per launch shape
+    // (cluster size, CTAs, CTA size, shared memory); each call captures its
+    // launch and updates the matching executable graph in place
+    std::map<std::tuple<int, int, int, size_t>, cudaGraphExec_t> b_graphs;
 
     void set_err(const std::string &s) { err = s; }
 };

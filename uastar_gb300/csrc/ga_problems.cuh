@@ -106,6 +106,24 @@ struct GridProblem : NarrowSlots {
         return g + h_of(key);  // field-wise: both halves stay below 2^31
     }
 
+    // Open bits of the cells (r, y-1), (r, y), (r, y+1) as bits 0..2 (0 for a
+    // row or column outside the grid).  Two 32-bit words cover the three
+    // cells, and their addresses depend on the cell alone, so the three rows
+    // of a node are read in one round trip of independent loads.
+    __device__ __forceinline__ uint32_t row3(int r, int y) const {
+        if (r < 0 || r >= H) return 0;
+        const int64_t c0 = (int64_t)r * W + y - 1;  // cell (r, y-1); -1 only for (0, 0)
+        const uint64_t lo = c0 < 0 ? 0 : (uint64_t)c0;
+        const uint64_t wlast = ((uint64_t)(uint32_t)H * (uint32_t)W + 63) / 64 * 2 - 1;  // last 32-bit word
+        const uint64_t w0 = lo >> 5, w1 = w0 + 1 <= wlast ? w0 + 1 : wlast;
+        const uint64_t v = (uint64_t)__ldg(bm + w0) | ((uint64_t)__ldg(bm + w1) << 32);
+        uint32_t bits = (uint32_t)(v >> (lo & 31u)) & 7u;
+        if (c0 < 0) bits = (bits << 1) & 7u;  // the window starts one cell before the grid
+        if (y == 0) bits &= ~1u;              // (r, -1) is no cell
+        if (y == W - 1) bits &= ~4u;          // (r, W) is no cell (the next row's first)
+        return bits;
+    }
+
     // Valid moves of a popped cell, bit i = direction i (4 straight, then 4
     // diagonal; src/utils.hpp:120-122).  Only an open cell moves
     // (CPU-solver.cpp:98-100).  A move into a blocked cell is legal in the
@@ -114,15 +132,14 @@ struct GridProblem : NarrowSlots {
     __device__ uint32_t moves(uint64_t key, uint32_t) const {
         const uint32_t c = (uint32_t)key;
         const int x = (int)(c / (uint32_t)W), y = (int)(c - (uint32_t)x * (uint32_t)W);
-        if (!open((int64_t)key)) return 0;
-        const int gx = ex, gy = ey;
+        const uint32_t rows[3] = {row3(x - 1, y), row3(x, y), row3(x + 1, y)};
+        if (!(rows[1] & 2u)) return 0;
         uint32_t m = 0;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-            const int nx = x + c_dx(i), ny = y + c_dy(i);
-            if (nx < 0 || nx >= H || ny < 0 || ny >= W) continue;
-            const int64_t nid = (int64_t)nx * W + ny;
-            if (open(nid) || (nx == gx && ny == gy)) m |= 1u << i;
+            const int dx = c_dx(i), dy = c_dy(i);
+            const bool goal = x + dx == ex && y + dy == ey;
+            if (((rows[dx + 1] >> (dy + 1)) & 1u) || goal) m |= 1u << i;
         }
         return m;
     }

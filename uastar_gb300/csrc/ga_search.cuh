@@ -713,7 +713,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                 uint32_t aux;
                 P::load_node(m.tab + e.slot, key, g, aux);
                 // where the entry names its node (grids), the neighbourhood
-                // reads start now, beside the node record's
+                // reads go out beside the node record's, in one round trip
                 uint32_t mv_pre = 0;
                 if constexpr (P::kEntryKey) mv_pre = prob.entry_moves(e);
                 const uint64_t fcur = prob.f_of(key, g, aux);

@@ -166,19 +166,36 @@ int32_t uastar_grid_screen(const uint64_t *words, int32_t H, int32_t W, int32_t 
     // neighbours).  A search that exhausts its component without meeting the
     // other endpoint proves the goal unreachable; if both outgrow `limit`
     // cells the endpoints are presumed connected.
-    if (!words || H <= 0 || W <= 0) return 0;
+    if (!words || H <= 0 || W <= 0 || limit < 0) return 0;
     const uint64_t s = (uint64_t)sx * W + sy, e = (uint64_t)ex * W + ey;
     if (s == e) return 1;
+    // Visited cells in a flat open-addressed set (linear probing, all-ones =
+    // free) sized to 4x the bound, so it never fills.
+    uint64_t cap = 64;
+    while (cap < 4 * (uint64_t)limit + 64) cap <<= 1;
+    std::vector<uint32_t> set(cap);
     for (int dir = 0; dir < 2; ++dir) {
         const uint64_t from = dir == 0 ? s : e, to = dir == 0 ? e : s;
+        std::fill(set.begin(), set.end(), 0xFFFFFFFFu);
+        int64_t nseen = 0;
+        auto insert = [&](uint32_t id) {
+            uint64_t h = ((uint64_t)id * 0x9E3779B97F4A7C15ull) >> 20;
+            for (;; ++h) {
+                uint32_t &slot = set[h & (cap - 1)];
+                if (slot == id) return false;
+                if (slot == 0xFFFFFFFFu) {
+                    slot = id;
+                    ++nseen;
+                    return true;
+                }
+            }
+        };
         std::vector<uint32_t> q;
-        std::vector<uint64_t> seen_keys;
-        std::unordered_set<uint32_t> seen;
         q.push_back((uint32_t)from);
-        seen.insert((uint32_t)from);
+        insert((uint32_t)from);
         bool overflow = false;
         for (size_t head = 0; head < q.size(); ++head) {
-            if ((int64_t)seen.size() > limit) {
+            if (nseen > limit) {
                 overflow = true;
                 break;
             }
@@ -191,7 +208,7 @@ int32_t uastar_grid_screen(const uint64_t *words, int32_t H, int32_t W, int32_t 
                 const uint64_t nid = (uint64_t)nx * W + ny;
                 if (dir == 1 && !bit_open(words, nid)) continue;  // predecessors must be open
                 if (nid == to) return 1;
-                if (seen.insert((uint32_t)nid).second) q.push_back((uint32_t)nid);
+                if (insert((uint32_t)nid)) q.push_back((uint32_t)nid);
             }
         }
         if (!overflow) return 0;

@@ -20,7 +20,15 @@
 //     each other; serialize them;
 //   - the first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress); make that first call outside any stream
-//     capture.
+//     capture.  The address is kept for the life of the process: after a
+//     cudaDeviceReset the array lives in a new context and this entry point
+//     must not be called again in that process;
+//   - every team-barrier wait of the search gives up after 10 s and the
+//     result then reports UASTAR_TIMEOUT;
+//   - a call that returns anything but UASTAR_OK queued nothing that writes
+//     the result record (its contents are unchanged); an error left pending
+//     by the caller's earlier CUDA work is reported as UASTAR_CUDA_ERROR and
+//     left pending, before anything is queued.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -138,6 +146,8 @@ extern "C" int32_t uastar_grid_solve_noalloc(const uint64_t *d_words, int32_t H,
     if (!d_words || !d_path || !d_result || path_cap < 1 || H <= 0 || W <= 0) return UASTAR_BAD_INPUT;
     if ((uint64_t)H * (uint64_t)W > kMaxCells) return UASTAR_BAD_INPUT;  // beyond the fixed scratch's maximum
     if (sx < 0 || sx >= H || sy < 0 || sy >= W || ex < 0 || ex >= H || ey < 0 || ey >= W) return UASTAR_BAD_INPUT;
+    // an error from the caller's earlier work is theirs: report it, keep it
+    if (cudaPeekAtLastError() != cudaSuccess) return UASTAR_CUDA_ERROR;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return UASTAR_CUDA_ERROR;
 
@@ -185,7 +195,7 @@ extern "C" int32_t uastar_grid_solve_noalloc(const uint64_t *d_words, int32_t H,
     m.cand = reinterpret_cast<Cand *>(scratch + kOffCand);
     m.max_rounds = 1ull << 31;
     TeamState *st = reinterpret_cast<TeamState *>(scratch + kOffState);
-    uint64_t timeout_ns = 10ull * 1000000000ull;
+    uint64_t timeout_ns = 10ull * 1000000000ull;  // bound on every team-barrier wait (UASTAR_TIMEOUT)
     void *args[] = {&prob, &m, &st, &timeout_ns};
     const size_t smem = SearchSmem<GridProblem>::bytes(kHeapsPerCta, kTopLevels);
     if (cudaLaunchCooperativeKernel((const void *)k_noalloc_search, dim3(kCtas), dim3(kBlock), args, smem, s) !=

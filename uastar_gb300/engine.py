@@ -249,6 +249,14 @@ class Engine:
     def kernel_launches(self) -> int:
         return int(self._lib.uastar_kernel_launches(self._h))
 
+    def round_floor(self, rounds: int = 2000) -> tuple[float, float]:
+        """Microseconds per round of a bare team barrier, and of one dependent
+        16-byte table CAS per thread plus the barrier, on this engine's plain
+        launch geometry (uastar_round_floor)."""
+        a, b = C.c_double(), C.c_double()
+        self._check(self._lib.uastar_round_floor(self._h, rounds, C.byref(a), C.byref(b)), "round_floor")
+        return a.value, b.value
+
     def set_stream(self, stream_ptr: int | None) -> None:
         self._lib.uastar_set_stream(self._h, C.c_void_p(stream_ptr or 0))
 
@@ -368,7 +376,9 @@ class Engine:
         arr = (L.Instance * len(insts))(*[_to_struct(i, keep) for i in insts])
         best = L.BatchConfig()
         self._check(self._lib.uastar_autotune(self._h, arr, len(insts), C.byref(best)), "autotune")
-        return {k: getattr(best, k) for k, _ in L.BatchConfig._fields_}
+        out = {k: getattr(best, k) for k, _ in L.BatchConfig._fields_}
+        out["tried"] = out.pop("reserved")  # configurations timed
+        return out
 
     # serving loop
     def serve_start(self, *, hbm_budget_gb: float = 120.0, slots: int = 0, threads_per_instance: int = 0,

@@ -120,18 +120,62 @@ def mixed_1024(n_puzzles: int = 768, n_grids: int = 256, seed: int = MIX_SEED, m
 
 
 def serve_stream(count: int, rate_per_s: float, seed: int = 0x5E57E, max_side: int = 8192,
-                 walks: tuple = (60, 300), min_side: int = 256):
-    """(arrival offset in seconds, spec) pairs: Poisson arrivals at `rate_per_s`."""
+                 walks: tuple = (60, 300), min_side: int = 256, workers: int = 0):
+    """(arrival offset in seconds, spec) pairs: Poisson arrivals at `rate_per_s`.
+
+    The request mix does not depend on the rate, only the arrival times do.
+    Grid seeds are screened for connected corners on `workers` threads (0 =
+    every host core; the screen runs in the C library, outside the GIL)."""
     t = 0.0
-    out = []
+    times, jobs = [], []
+    table = _screen_table(seed, max_side, walks, min_side)
     for i in range(count):
         u = uniform(seed, 4 * i)
         t += -math.log(1.0 - u) / rate_per_s
+        times.append(t)
         if uniform(seed, 4 * i + 1) < 0.5:
-            spec = PuzzleSpec(4, randint(seed, 4 * i + 2, walks[0], walks[1]), splitmix64(seed ^ 0x77, i))
+            jobs.append(PuzzleSpec(4, randint(seed, 4 * i + 2, walks[0], walks[1]), splitmix64(seed ^ 0x77, i)))
         else:
             side = randint(seed, 4 * i + 2, min_side, max_side)
             r = round(0.10 + 0.30 * uniform(seed, 4 * i + 3), 4)
-            spec = screened_grid(side, side, r, splitmix64(seed ^ 0x99, i) & 0xFFFFFFFF)
-        out.append((t, spec))
-    return out
+            s0 = splitmix64(seed ^ 0x99, i) & 0xFFFFFFFF
+            if table is not None and i < table[0]:
+                jobs.append(GridSpec(side, side, r, s0 + table[1].get(i, 0)))
+            else:
+                jobs.append((side, r, s0))
+    specs = parallel_map(lambda j: j if isinstance(j, (PuzzleSpec, GridSpec)) else
+                         screened_grid(j[0], j[0], j[1], j[2]), jobs, workers)
+    return list(zip(times, specs))
+
+
+_SCREEN = {}
+
+
+def _screen_table(seed, max_side, walks, min_side):
+    """(count, {index: seeds skipped}) of the recorded screen of the default
+    serving stream (serve_stream_screen.json, made by screened_grid on every
+    grid of its first `count` requests; a test re-screens a sample), or None
+    for any other stream."""
+    import json
+    from pathlib import Path
+    if "t" not in _SCREEN:
+        p = Path(__file__).with_name("serve_stream_screen.json")
+        _SCREEN["t"] = json.loads(p.read_text()) if p.exists() else None
+    t = _SCREEN["t"]
+    if t is None or t["stream"] != {"seed": seed, "max_side": max_side, "min_side": min_side,
+                                    "walks": list(walks)}:
+        return None
+    return t["count"], {int(k): v for k, v in t["offsets"].items()}
+
+
+def parallel_map(fn, items, workers: int = 0):
+    """fn over items on a thread pool, results in order (the generators and
+    screens are C calls that release the GIL)."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+    items = list(items)
+    n = workers if workers > 0 else (os.cpu_count() or 1)
+    if n <= 1 or len(items) < 2:
+        return [fn(x) for x in items]
+    with ThreadPoolExecutor(min(n, len(items))) as ex:
+        return list(ex.map(fn, items))
