@@ -691,7 +691,7 @@ def run_case(args) -> None:
     c = args.case
     if c in ("grid_1000", "grid_20000", "grid_4096"):
         sp = {"grid_1000": WL.GRID_1000, "grid_20000": WL.GRID_20000,
-              "grid_4096": WL.GridSpec(4096, 4096, 0.30, 7)}[c]
+              "grid_4096": WL.screened_grid(4096, 4096, 0.30, 7)}[c]
         log2 = {"grid_1000": 22, "grid_20000": 28, "grid_4096": 25}[c]
         words = sp.words()
         # fixed tables: one search launch per solve (no in-place growth)
@@ -725,15 +725,16 @@ def run_case(args) -> None:
             for _ in range(args.repeat):
                 print(f"pdb4: built in {eng.pdb_build(4):.1f} ms", flush=True)
     elif c == "grow":
-        # an auto-sized table that starts at 2^20 slots and grows in place
-        # (k_grow_move / k_grow_links / k_grow_heaps) on a 4096^2 grid
-        sp = WL.GridSpec(4096, 4096, 0.30, 7)
-        words = sp.words()
-        with Engine(0, heaps=8192, block_threads=256, threads_per_heap=4) as eng:
+        # an auto-sized dedup table that starts at 2^22 slots and grows in
+        # place (k_grow_move / k_grow_links / k_grow_heaps) when half full:
+        # a 15-puzzle whose search stores ~4 M states (200-move walk, seed 1039)
+        with Engine(0) as eng:
+            eng.pdb_build(4)
+            tiles = WL.PuzzleSpec(4, 200, 1039).tiles()
             for _ in range(args.repeat):
-                r = eng.grid_solve(words, sp.H, sp.W, sp.start, sp.goal)
-                print(f"grow: {r.straight}+{r.diagonal}*sqrt2, {r.table_grows} table growths, "
-                      f"{r.table_used} slots in use, kernel {r.kernel_ms:.1f} ms", flush=True)
+                r = eng.puzzle_solve(4, tiles)
+                print(f"grow: {r.steps} moves, {r.table_grows} table growths, {r.table_used} slots in use, "
+                      f"kernel {r.kernel_ms:.1f} ms", flush=True)
     elif c == "migrate":
         # serving requests whose frontier outgrows one CTA move to cluster
         # slots with their search state (k_migrate_heaps)
@@ -742,11 +743,14 @@ def run_case(args) -> None:
         with Engine(0) as eng:
             eng.pdb_build(4)
             for _ in range(args.repeat):
-                eng.serve_start(hbm_budget_gb=16.0)
+                eng.serve_start(hbm_budget_gb=4.0)
                 for s in specs:
                     eng.serve_submit(s.instance())
-                st = eng.serve_stop(120.0)
-                res = eng.serve_poll()
+                res, t0 = [], time.time()
+                while len(res) < len(specs) and time.time() - t0 < 120:
+                    res += eng.serve_poll()
+                    time.sleep(0.002)
+                st = eng.serve_stop(10.0)
                 print(f"migrate: {sum(r['status'] == 0 for _, r in res)}/{len(res)} ok, "
                       f"{sum(r['migrations'] for _, r in res)} migrations, {st['quanta']} quanta", flush=True)
     elif c == "bounded":
@@ -758,8 +762,9 @@ def run_case(args) -> None:
                 r = eng.puzzle_solve_bounded(4, tiles, 20)
                 print(f"bounded: {r['steps']} moves, bound {r['lower_bound']}, {r['segments']} segments", flush=True)
     elif c == "walk":
-        # path walks after solves: k_walk on a 4096^2 grid, k_batch_walk in a batch
-        sp = WL.GridSpec(4096, 4096, 0.30, 7)
+        # path walks after solves: k_walk on a 4096^2 grid, the in-kernel
+        # walk of a batch
+        sp = WL.screened_grid(4096, 4096, 0.30, 7)
         words = sp.words()
         grids = [WL.screened_grid(1024, 1024, 0.25, 60 + i, exact=True).instance() for i in range(16)]
         with Engine(0, heaps=8192, block_threads=256, threads_per_heap=4, hash_log2_slots=25) as eng:
