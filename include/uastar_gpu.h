@@ -304,11 +304,15 @@ typedef struct {
     int32_t threads_per_instance;
     int32_t threads_per_heap;
     int32_t heap_capacity;
-    int32_t rounds_per_quantum; /* GA* rounds per persistent-kernel launch (0 -> 256) */
+    int32_t rounds_per_quantum; /* cap on GA* rounds per persistent-kernel launch (0 -> 65536 with
+                                   a time slice, 256 without) */
     double load_factor;
     int32_t cluster_slots;    /* cap on 8-CTA slots for requests whose search outgrows one CTA
                                  (0 -> as many as fit, -1 -> none) */
-    int32_t reserved;
+    int32_t quantum_us;       /* time slice of a persistent-kernel launch: every resident search
+                                 runs rounds until this many microseconds have passed since the
+                                 launch began, so that fast and slow searches share the GPU's time
+                                 rather than a round count (0 -> 4000; < 0 -> none, rounds only) */
 } uastar_serve_config;
 
 typedef struct {

@@ -220,19 +220,49 @@ def serve_sample(stream, n_big: int = 64, n_long: int = 64, n_rest: int = 384):
     return sorted(chosen | set(rest[:n_rest]))
 
 
-def part_c5(jobs=8, puzzle_jobs=4):
+def ref_puzzle_one(n: int, board, tag: str, timeout_s: float, mem_gb: float):
+    """The reference's CPU A* on one board in its own process, bounded in
+    time and address space; None when it does not finish within them."""
+    import resource
+
+    def limit():
+        b = int(mem_gb * (1 << 30))
+        resource.setrlimit(resource.RLIMIT_AS, (b, b))
+
+    inp, outp = WORK / f"{tag}.txt", WORK / f"{tag}.jsonl"
+    inp.write_text(" ".join(map(str, board)) + "\n")
+    try:
+        subprocess.run([str(REF / "ref_puzzle"), "solve", str(n), str(PDB_DIR), str(inp), str(outp)], check=True,
+                       capture_output=True, timeout=timeout_s, preexec_fn=limit)
+        rows = [json.loads(x) for x in outp.read_text().splitlines() if x.strip()]
+        return rows[0] if rows and rows[0].get("solved") else None
+    except (subprocess.CalledProcessError, subprocess.TimeoutExpired):
+        return None
+    finally:
+        inp.unlink(missing_ok=True)
+        outp.unlink(missing_ok=True)
+
+
+def part_c5(jobs=6, puzzle_jobs=4, timeout_s=900.0, mem_gb=12.0):
+    """The serving stream's golden sample.  Each puzzle is solved by the
+    reference in its own process within `timeout_s` and `mem_gb`; a board
+    that needs more is recorded as skipped (ref.solved false, with the
+    reason) and left out of the comparisons."""
     stream = WL.serve_stream(20000, 1.0)
     idx = serve_sample(stream)
     pz = [i for i in idx if isinstance(stream[i][1], WL.PuzzleSpec)]
     gr = [i for i in idx if isinstance(stream[i][1], WL.GridSpec)]
-    pres = ref_puzzle_parallel(4, [stream[i][1].tiles().tolist() for i in pz], "c5p", puzzle_jobs)
     rows = {}
-    for i, r in zip(pz, pres):
-        s = stream[i][1]
-        rows[i] = {"index": i, "kind": "puzzle", "seed": s.seed, "walk": s.walk,
-                   "ref": {k: r[k] for k in ("solved", "steps", "stored", "solve_seconds")}}
 
-    def one(i):
+    def one_puzzle(i):
+        s = stream[i][1]
+        r = ref_puzzle_one(4, s.tiles().tolist(), f"c5p_{i}", timeout_s, mem_gb)
+        ref = ({k: r[k] for k in ("solved", "steps", "stored", "solve_seconds")} if r else
+               {"solved": False, "skipped": f"the reference's CPU A* needs more than {timeout_s:.0f} s or "
+                                             f"{mem_gb:.0f} GB for this board"})
+        return {"index": i, "kind": "puzzle", "seed": s.seed, "walk": s.walk, "ref": ref}
+
+    def one_grid(i):
         s = stream[i][1]
         rec = grid_case(f"c5_{i}", s.words(), s.H, s.W, s.start, s.goal,
                         {"kind": "random", "rate": s.rate, "seed": s.seed}, keep_path=False)
@@ -240,8 +270,12 @@ def part_c5(jobs=8, puzzle_jobs=4):
         rec["index"] = i
         return rec
 
+    with cf.ThreadPoolExecutor(puzzle_jobs) as ex:
+        for rec in ex.map(one_puzzle, pz):
+            rows[rec["index"]] = rec
+            print("puzzle", rec["index"], rec["ref"].get("steps"), flush=True)
     with cf.ThreadPoolExecutor(jobs) as ex:
-        for rec in ex.map(one, gr):
+        for rec in ex.map(one_grid, gr):
             rows[rec["index"]] = rec
     (GOLDEN / "serve_c5_sample.json").write_text(json.dumps([rows[i] for i in idx], indent=0))
 

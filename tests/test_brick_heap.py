@@ -1,5 +1,6 @@
 """The cache-line-blocked binary heap of the search kernel
-(ga_search.cuh BrickHeap / heap_sift_down / heap_push / heap_geometry),
+(ga_search.cuh BrickHeap / heap_sift_down / heap_push / heap_push_run /
+heap_geometry),
 restated in Python and fuzzed against heapq: the index -> global offset map
 is a bijection into the heap's block, and pops return the minimum."""
 from __future__ import annotations
@@ -76,6 +77,63 @@ class BrickHeap:
             self.st(now, pv)
             now = par
         self.st(now, v)
+
+    def climb(self, now, v):
+        """heap_climb: fill the vacant position `now` with v."""
+        while now > 1:
+            par = now >> 1
+            pv = self.ld(par)
+            if not v < pv:
+                break
+            self.st(now, pv)
+            now = par
+        self.st(now, v)
+
+    def push_run(self, vals):
+        """heap_push_run: the bottom brick read once and kept across the run."""
+        D, L, topn = self.D, self.L, self.topn()
+        cached, b = None, None
+
+        def flush():
+            nonlocal cached
+            if cached is not None:
+                base = self.reserve + off(cached, D, L) - 1
+                self.g[base:base + (1 << D)] = b
+                cached = None
+
+        for x in vals:
+            now = self.size + 1
+            if now <= topn:
+                self.push(x)
+                continue
+            self.size = now
+            r = now.bit_length() - 1 - L
+            d = r % D
+            root = now >> d
+            if root != cached:
+                flush()
+                # a bottom position that roots its own brick: nothing to read
+                b = list(self.fetch(root)) if d > 0 else [None] * (1 << D)
+                cached = root
+            loc = (1 << d) | (now & ((1 << d) - 1))
+            while loc > 1:
+                pv = b[loc >> 1]
+                if not x < pv:
+                    break
+                b[loc] = pv
+                loc >>= 1
+                now >>= 1
+            if loc > 1:
+                b[loc] = x
+                continue
+            pv = self.ld(now >> 1)
+            if not x < pv:
+                b[1] = x
+                continue
+            b[1] = pv
+            flush()
+            self.climb(now >> 1, x)
+        flush()
 
     def pop(self):
         out = self.s[1]
@@ -177,3 +235,41 @@ def test_sift_waits_on_global_memory_once_per_brick():
     # depth ~13 with 4 shared levels: ~3 brick bursts + the tail load per pop,
     # against ~9 dependent loads for an unblocked layout
     assert h.loads / 100 <= 2 * 4 + 1
+
+
+@pytest.mark.parametrize("D,L", [(3, 1), (3, 3), (4, 2), (4, 5), (3, 7)])
+def test_pushed_runs_match_heapq(D, L):
+    # drains of 1..8 entries between pops, as the owners' chores do
+    rng = random.Random(D * 7 + L)
+    h = BrickHeap(D, L, 4000)
+    ref = []
+    for step in range(6000):
+        if ref and rng.random() < 0.4:
+            assert h.pop() == heapq.heappop(ref)
+        elif h.size + 8 < h.hcap:
+            run = [(rng.randrange(500), rng.randrange(1 << 20)) for _ in range(rng.randrange(1, 9))]
+            h.push_run(run)
+            for v in run:
+                heapq.heappush(ref, v)
+        assert h.size == len(ref)
+    while ref:
+        assert h.pop() == heapq.heappop(ref)
+
+
+def test_a_run_reads_its_bottom_brick_once():
+    # D = 4, L = 3: positions 64..127 sit at depth 3 of bricks of 8 siblings
+    # (rooted at 8..15); large entries climb nowhere, so a run of 4 into
+    # positions 73..76 reads one brick
+    h = BrickHeap(4, 3, 1 << 14)
+    for i in range(72):
+        h.push((i,))
+    h.loads = 0
+    h.push_run([(10 ** 6 + i,) for i in range(4)])
+    assert h.loads == 1
+    # positions 3001..3004 each root a brick of their own: no brick read,
+    # only the parent that each entry is compared with
+    for i in range(72, 3000):
+        h.push((i,))
+    h.loads = 0
+    h.push_run([(10 ** 6 + i,) for i in range(4)])
+    assert h.loads == 4

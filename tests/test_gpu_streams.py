@@ -50,7 +50,10 @@ def test_full_mixed_batch_matches_reference(eng4):
 def test_serving_sample_matches_reference(eng4):
     rows = golden("serve_c5_sample.json")
     stream = WL.serve_stream(20000, 1.0)
-    sample = [(r["index"], r) for r in rows]
+    # boards the reference's CPU A* could not finish within the fixture
+    # script's time and memory bounds carry no reference result
+    sample = [(r["index"], r) for r in rows if r["ref"].get("solved")]
+    assert len(sample) >= 256
     for i, row in sample:
         s = stream[i][1]
         assert row["seed"] == s.seed and row["kind"] == ("puzzle" if isinstance(s, WL.PuzzleSpec) else "grid")

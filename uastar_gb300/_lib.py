@@ -82,7 +82,7 @@ class BatchStats(C.Structure):
 class ServeConfig(C.Structure):
     _fields_ = [("hbm_budget_gb", C.c_double), ("slots", C.c_int32), ("threads_per_instance", C.c_int32),
                 ("threads_per_heap", C.c_int32), ("heap_capacity", C.c_int32), ("rounds_per_quantum", C.c_int32),
-                ("load_factor", C.c_double), ("cluster_slots", C.c_int32), ("reserved", C.c_int32)]
+                ("load_factor", C.c_double), ("cluster_slots", C.c_int32), ("quantum_us", C.c_int32)]
 
 
 class ServeCompletion(C.Structure):

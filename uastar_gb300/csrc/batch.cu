@@ -85,6 +85,7 @@ struct BatchArgs {
     uint64_t budget;       // rounds per call (serving quantum) or ~0
     int serving;           // 1: CTA b serves slot b; 0: work queue
     uint64_t region_slots; // batch: dedup region of each team (reused by the instances it takes)
+    uint64_t quantum_ns;   // serving: time slice of the launch, from each team's start (0: rounds only)
     unsigned long long *keys;  // batch: path keys of solved instances
 };
 
@@ -116,7 +117,8 @@ __device__ void init_state(TeamState *st) { team_state_init(st); }
 // Runs one instance on this CTA for up to `budget` rounds.
 template <class Team>
 __device__ uint32_t run_instance(const BatchArgs &a, const InstDesc &d, Team &team, Slot *tab, uint8_t *heaps,
-                                 uint32_t *hs, Cand *cand, unsigned char *smem, uint64_t budget) {
+                                 uint32_t *hs, Cand *cand, unsigned char *smem, uint64_t budget,
+                                 uint64_t deadline_ns) {
     const uint64_t slots = 1ull << d.log2_slots;
     const bool own_geo = a.serving != 0;  // serving requests carry their heap geometry
     if (d.kind == UASTAR_KIND_GRID) {
@@ -133,6 +135,7 @@ __device__ uint32_t run_instance(const BatchArgs &a, const InstDesc &d, Team &te
                                own_geo ? d.heap_stride : a.stride_grid, own_geo ? d.heap_hcap : a.hcap_grid,
                                a.L_grid, hs, cand, d.max_rounds};
         if (d.grow_at) m.grow_at = d.grow_at;
+        m.deadline_ns = deadline_ns;
         return ga_search(prob, team, m, a.H, smem, budget);
     }
     SearchMem<PuzzleEntry> m{tab, slots - 1, (uint64_t)(slots * a.max_load), 4096u,
@@ -140,6 +143,7 @@ __device__ uint32_t run_instance(const BatchArgs &a, const InstDesc &d, Team &te
                              own_geo ? d.heap_stride : a.stride_puzzle, own_geo ? d.heap_hcap : a.hcap_puzzle,
                              a.L_puzzle, hs, cand, d.max_rounds};
     if (d.grow_at) m.grow_at = d.grow_at;
+    m.deadline_ns = deadline_ns;
     if (d.n == 4) {
         PuzzleProblem<4> prob;
         prob.pdb = a.pdb4;
@@ -190,7 +194,8 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
         }
         __syncthreads();
         BlockTeam team{&st};
-        run_instance(a, d, team, tab, heaps, hs, cand, smem, d.budget ? d.budget : a.budget);
+        run_instance(a, d, team, tab, heaps, hs, cand, smem, d.budget ? d.budget : a.budget,
+                     a.quantum_ns ? t_start + a.quantum_ns : 0);
         __syncthreads();
         if (threadIdx.x == 0) {
             InstOut o;
@@ -264,7 +269,8 @@ __global__ void __launch_bounds__(512, 1) k_batch_cluster(BatchArgs a) {
             if (crank == 0 && threadIdx.x == 0) init_state(st);
         }
         team.sync();
-        run_instance(a, d, team, tab, heaps, hs, cand, smem, d.budget ? d.budget : a.budget);
+        run_instance(a, d, team, tab, heaps, hs, cand, smem, d.budget ? d.budget : a.budget,
+                     a.quantum_ns ? t_start + a.quantum_ns : 0);
         team.sync();
         if (crank == 0 && threadIdx.x == 0) {
             InstOut o;
@@ -1251,7 +1257,11 @@ static BatchArgs serve_args(ServeState *S, ServeTier &t) {
     a.H = t.geo.H;
     a.L_grid = t.geo.L_grid;
     a.L_puzzle = t.geo.L_puzzle;
-    a.budget = (uint64_t)(S->cfg.rounds_per_quantum > 0 ? S->cfg.rounds_per_quantum : 256);
+    // a time slice per launch (every resident search runs until it has
+    // passed), capped by a round count; or, without a slice, the round count
+    const bool sliced = S->cfg.quantum_us >= 0;
+    a.quantum_ns = sliced ? (uint64_t)(S->cfg.quantum_us > 0 ? S->cfg.quantum_us : 4000) * 1000ull : 0;
+    a.budget = (uint64_t)(S->cfg.rounds_per_quantum > 0 ? S->cfg.rounds_per_quantum : sliced ? 65536 : 256);
     a.serving = 1;
     a.keys = t.d_keys.as<unsigned long long>();
     return a;

@@ -117,6 +117,8 @@ struct __align__(16) TeamState {
     unsigned long long ins[3];        // dedup slots claimed in the round
     uint32_t err[3];                  // first error of the round's relax phase
     uint32_t pad0_;
+    uint32_t quit[3];                 // the round ended past the search's time slice (SearchMem::deadline_ns)
+    uint32_t pad1_;
     // totals, stored by CTA 0 when the search stops or pauses
     unsigned long long goal_best;     // best goal f popped so far
     unsigned long long round;         // rounds completed

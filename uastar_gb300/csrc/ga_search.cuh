@@ -73,6 +73,11 @@ template <class E> struct SearchMem {
     // and no work in flight, so that the host can move the table to a larger
     // one and resume; ~0 = never.
     uint64_t grow_at = ~0ull;
+    // A time slice: the search also pauses at the end of the first round
+    // that team rank 0 finishes at or after this globaltimer value (ns);
+    // 0 = none.  The serving loop's quanta end on it, so that every resident
+    // search runs for the same time rather than the same number of rounds.
+    uint64_t deadline_ns = 0;
     // Sort-based dedup (ga_search<.., true>): every round's successors are
     // radix-sorted by key and each key's minimum-g record is relaxed once.
     unsigned long long *sort_buf = nullptr;  // 2 x C * H * kMoves pairs
@@ -251,23 +256,27 @@ __device__ __forceinline__ void heap_sift_down(const BrickHeap<P> &h, uint32_t s
     h.st(now, last);
 }
 
-// Insert v.  Below the shared top the climb works brick by brick: the brick
-// holding the current position is read once (one burst of independent loads)
-// into scratch half 0, the climb inside it runs in shared memory and the
-// brick is written back, so a push waits on global memory once per brick it
-// climbs through (most climb none or one) instead of once per level.
+// Fill the vacant heap position `now` with v, moving v up as far as it goes.
+// Below the shared top the climb works brick by brick: the brick holding the
+// current position is read once (one burst of independent loads) into
+// scratch half 0, the climb inside it runs in shared memory and the brick is
+// written back, so a climb waits on global memory once per brick it passes
+// through (most pass none or one) instead of once per level.  `bottom`: `now`
+// is the heap's new last position, so a brick rooted there holds nothing
+// else yet (all its other positions are below it) and is not read.
 template <class P>
-__device__ __forceinline__ void heap_push(const BrickHeap<P> &h, uint32_t &size, const typename P::Entry &v) {
+__device__ __forceinline__ void heap_climb(const BrickHeap<P> &h, uint32_t now, const typename P::Entry &v,
+                                           bool bottom = false) {
     using E = typename P::Entry;
     constexpr uint32_t D = BrickHeap<P>::D;
-    uint32_t now = ++size;
     const uint32_t topn = h.topn();
     while (now > topn) {
         const uint32_t l = 31u - (uint32_t)__clz(now);
         const uint32_t r = l - h.L;
         const uint32_t d = r - (r / D) * D;  // depth of `now` in its brick
         const uint32_t root = now >> d;
-        h.fetch(root, 0);
+        if (!(bottom && d == 0)) h.fetch(root, 0);
+        bottom = false;
         E *const b = h.scr;
         uint4 *const gl = reinterpret_cast<uint4 *>(h.g + h.off(root) - 1);
         uint32_t loc = (1u << d) | (now & ((1u << d) - 1u));
@@ -303,6 +312,80 @@ __device__ __forceinline__ void heap_push(const BrickHeap<P> &h, uint32_t &size,
         now = par;
     }
     h.s[now] = v;
+}
+
+// Insert v.
+template <class P>
+__device__ __forceinline__ void heap_push(const BrickHeap<P> &h, uint32_t &size, const typename P::Entry &v) {
+    heap_climb<P>(h, ++size, v, true);
+}
+
+// Insert the n entries at v (an insertion buffer's drain).  They take the
+// positions size+1 .. size+n, consecutive leaves at the bottom of the tree
+// that share one brick (two at a brick or level boundary): that brick is
+// read once into scratch half 1, every entry's climb inside it runs there,
+// and it is written back when the bottom moves to another brick, before a
+// climb that leaves it (finished by heap_climb from the brick above), and at
+// the end.  A drain of n entries so waits on global memory about once
+// instead of n times.  (A bottom position that roots its own brick needs no
+// read: nothing else in that brick is in use.)
+template <class P>
+__device__ __forceinline__ void heap_push_run(const BrickHeap<P> &h, uint32_t &size, const typename P::Entry *v,
+                                              uint32_t n) {
+    using E = typename P::Entry;
+    constexpr uint32_t D = BrickHeap<P>::D, BE = BrickHeap<P>::BE;
+    const uint32_t topn = h.topn();
+    E *const b = h.scr + BE;  // scratch half 1
+    uint32_t cached = 0;      // root of the brick held in b (0: none)
+    const auto flush = [&]() {
+        if (!cached) return;
+        uint4 *const gl = reinterpret_cast<uint4 *>(h.g + h.off(cached) - 1);
+        const uint4 *src = reinterpret_cast<const uint4 *>(b);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) gl[q] = src[q];
+        cached = 0;
+    };
+    for (uint32_t i = 0; i < n; ++i) {
+        const E x = v[i];
+        uint32_t now = size + 1;
+        if (now <= topn) {  // shared top only: no brick involved
+            heap_push<P>(h, size, x);
+            continue;
+        }
+        size = now;
+        const uint32_t l = 31u - (uint32_t)__clz(now);
+        const uint32_t r = l - h.L;
+        const uint32_t d = r - (r / D) * D;
+        const uint32_t root = now >> d;
+        if (root != cached) {
+            flush();
+            if (d > 0) h.fetch(root, 1);
+            cached = root;
+        }
+        uint32_t loc = (1u << d) | (now & ((1u << d) - 1u));
+        while (loc > 1) {
+            const E pv = b[loc >> 1];
+            if (!P::less(x, pv)) break;
+            b[loc] = pv;
+            loc >>= 1;
+            now >>= 1;
+        }
+        if (loc > 1) {
+            b[loc] = x;
+            continue;
+        }
+        // at the brick's root: its parent is in the brick above or the shared
+        // top, neither of which is cached
+        const E pv = h.ld(now >> 1);
+        if (!P::less(x, pv)) {
+            b[1] = x;
+            continue;
+        }
+        b[1] = pv;
+        flush();
+        heap_climb<P>(h, now >> 1, x);
+    }
+    flush();
 }
 
 // Global entries per heap and the largest heap size for L shared levels and
@@ -774,18 +857,25 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         // entries (room for this round's pushes).
         const auto chores = [&]() {
             if (pending_sift) heap_sift_down<P>(myheap, hs, last);
-            while (bn > kBuf - P::kMoves) {
-                if (hs + 1 > m.hcap) {
+            if (bn > kBuf - P::kMoves) {
+                // move the buffer's largest entries (the small ones are
+                // popped soon) to its end, then push them as one run
+                uint32_t run = bn - (kBuf - P::kMoves);
+                if (hs + run > m.hcap) {
                     set_error(&st->err[r3], ST_HEAP_OVERFLOW);  // this round's decision stops the search
-                    break;
+                    run = m.hcap > hs ? m.hcap - hs : 0u;
                 }
-                // move the buffer's largest entry (the small ones are popped soon)
-                uint32_t bx = 0;
-                for (uint32_t j = 1; j < bn; ++j)
-                    if (P::less(ibuf[bx], ibuf[j])) bx = j;
-                const E e = ibuf[bx];
-                ibuf[bx] = ibuf[--bn];
-                heap_push<P>(myheap, hs, e);
+                for (uint32_t q = 0; q < run; ++q) {
+                    const uint32_t end = bn - 1 - q;
+                    uint32_t bx = 0;
+                    for (uint32_t j = 1; j <= end; ++j)
+                        if (P::less(ibuf[bx], ibuf[j])) bx = j;
+                    const E e = ibuf[bx];
+                    ibuf[bx] = ibuf[end];
+                    ibuf[end] = e;
+                }
+                heap_push_run<P>(myheap, hs, ibuf + (bn - run), run);
+                bn -= run;
             }
         };
         if (rfirst > 0 && owner) chores();
@@ -880,6 +970,9 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         if (tid == 0) {
             half[(size_t)cta * RR].slot = kSort ? total : *s_cnt;
             if (*s_ins) atomicAdd(&st->ins[r3], (unsigned long long)*s_ins);
+            // the time slice is read by one thread of the team, so that all
+            // threads take the same decision
+            if (cta == 0 && m.deadline_ns) st->quit[r3] = globaltimer_ns() >= m.deadline_ns ? 1u : 0u;
         }
         team.sync();
 
@@ -901,7 +994,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         if (!err) err = team.rd32(&st->error);
         ins_total += team.rd64(&st->ins[r3]);
         if (!err && ins_total > m.max_inserted) err = ST_HASH_FULL;
-        const bool pause = ins_total > m.grow_at;
+        const bool pause = ins_total > m.grow_at || (m.deadline_ns && team.rd32(&st->quit[r3]));
         round += 1;
         if (err) {
             status = err;
@@ -927,6 +1020,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
             st->goal_min[a] = kInfCost;
             st->ins[a] = 0;
             st->err[a] = 0;
+            st->quit[a] = 0;
         }
         // This CTA's share of the round's candidates is the whole region of
         // CTA (c + round) mod C: the successors of that CTA's H pops, a

@@ -383,9 +383,9 @@ class Engine:
     # serving loop
     def serve_start(self, *, hbm_budget_gb: float = 120.0, slots: int = 0, threads_per_instance: int = 0,
                     threads_per_heap: int = 0, heap_capacity: int = 0, rounds_per_quantum: int = 0,
-                    load_factor: float = 0.0, cluster_slots: int = 0) -> None:
+                    load_factor: float = 0.0, cluster_slots: int = 0, quantum_us: int = 0) -> None:
         cfg = L.ServeConfig(hbm_budget_gb, slots, threads_per_instance, threads_per_heap, heap_capacity,
-                            rounds_per_quantum, load_factor, cluster_slots, 0)
+                            rounds_per_quantum, load_factor, cluster_slots, quantum_us)
         self._check(self._lib.uastar_serve_start(self._h, C.byref(cfg)), "serve_start")
 
     def serve_submit(self, inst, arrival_s: float = 0.0) -> int:
