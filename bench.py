@@ -582,11 +582,13 @@ def section_mb(eng, args):
     ensure_pdb(eng)
     tiles = WL.mixed_1024()[127].tiles()
     out = []
+    exact = lambda r: {"exact_passes": r["exact_passes"], "exact_optimal": bool(r["exact_optimal"]),
+                       "exact_nodes": r["exact_nodes"], "exact_ms": round(r["exact_ms"], 1)}
     for log2 in (20, 22, 24):
         r = eng.puzzle_solve_bounded(4, tiles, log2)
         out.append({"max_table_slots": 1 << log2, "table_mb": (1 << log2) * 32 >> 20, "status": r["status"],
                     "steps": r["steps"], "lower_bound": r["lower_bound"], "segments": r["segments"],
-                    "expanded": r["expanded"], "solve_ms": round(r["solve_ms"], 1)})
+                    "expanded": r["expanded"], "solve_ms": round(r["solve_ms"], 1), **exact(r)})
     opt = eng.puzzle_solve(4, tiles)
     for row in out:
         row["optimal_steps"] = opt.steps
@@ -597,7 +599,8 @@ def section_mb(eng, args):
         r = eng.puzzle_solve_bounded(5, t5, log2)
         out.append({"puzzle": "5x5, 400-move walk", "max_table_slots": 1 << log2, "table_mb": (1 << log2) * 32 >> 20,
                     "status": r["status"], "steps": r["steps"], "lower_bound": r["lower_bound"],
-                    "segments": r["segments"], "expanded": r["expanded"], "solve_ms": round(r["solve_ms"], 1)})
+                    "segments": r["segments"], "expanded": r["expanded"], "solve_ms": round(r["solve_ms"], 1),
+                    **exact(r)})
     return out
 
 

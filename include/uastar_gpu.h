@@ -73,7 +73,8 @@ typedef struct {
                                  successors are radix-sorted by cell on the device and each cell's
                                  least-g record is relaxed once.  Same results; puzzles always use 0
                                  (the reference's puzzle kernel probes its table per successor) */
-    int32_t reserved;
+    int32_t exact_ms;         /* memory-bounded mode: time for its exact (IDA*) passes after the
+                                 segments (0 -> 3000 ms, < 0 -> none) */
 } uastar_config;
 
 /* Replaces GPUPathwaySolver/GPUPuzzleSolver construction + initialize()'s
@@ -197,23 +198,31 @@ int64_t uastar_puzzle_moves(uastar_engine *eng, int32_t *moves, int64_t cap);
 
 /* Memory-bounded solve for puzzles too large for the dedup table (the
  * reference's README.md:30-34 describes such a mode; it has no code for it).
- * The search runs in segments of exact GA* with the table capped at
+ * Phase 1 runs segments of exact GA* with the table capped at
  * 2^max_log2_slots slots (32 B each).  A segment that fills the table pauses;
  * the open list's minimum f is then a lower bound on the remaining optimum,
  * the search commits to the open node holding it and the next segment starts
- * there.  The heuristic stays admissible throughout.  The result's steps are
- * the returned solution's length, lower_bound the first segment's bound on
- * the optimum (equal to steps when one segment sufficed: the solution is
- * then optimal).  Moves via uastar_puzzle_moves. */
+ * there; one segment means the solution is optimal.  Phase 2, when phase 1
+ * took more than one segment, runs iterative-deepening A* passes (depth-first
+ * search below a threshold on f, memory proportional to the depth, not to the
+ * table) from the first segment's bound upward, for at most uastar_config.
+ * exact_ms: a pass that finds a goal returns an optimal solution (steps =
+ * lower_bound, exact_optimal = 1); a pass that completes without one raises
+ * the bound; reaching phase 1's length proves that solution optimal.  The
+ * heuristic stays admissible throughout.  Moves via uastar_puzzle_moves. */
 typedef struct {
     int32_t status;
     int32_t steps;            /* moves of the returned solution */
-    int32_t lower_bound;      /* proven lower bound on the optimal move count */
-    int32_t segments;         /* exact searches run; 1 = the solution is optimal */
+    int32_t lower_bound;      /* proven lower bound on the optimal move count (= steps: optimal) */
+    int32_t segments;         /* table-capped GA* segments run; 1 = that solution is optimal */
     int64_t expanded;
     int64_t generated;
     double kernel_ms;
     double solve_ms;
+    int32_t exact_passes;     /* IDA* threshold passes run after the segments */
+    int32_t exact_optimal;    /* 1 if the passes proved the returned solution optimal */
+    int64_t exact_nodes;      /* nodes the passes generated */
+    double exact_ms;          /* their time */
 } uastar_bounded_result;
 
 int32_t uastar_puzzle_solve_bounded(uastar_engine *eng, int32_t n, const uint8_t *tiles, int32_t max_log2_slots,
@@ -303,7 +312,7 @@ typedef struct {
     int32_t slots;            /* max concurrently resident requests (0 -> all CTAs) */
     int32_t threads_per_instance;
     int32_t threads_per_heap;
-    int32_t heap_capacity;
+    int32_t heap_capacity;    /* entries per heap of a CTA slot (0 -> 16383; 4x on overflow) */
     int32_t rounds_per_quantum; /* cap on GA* rounds per persistent-kernel launch (0 -> 65536 with
                                    a time slice, 256 without) */
     double load_factor;

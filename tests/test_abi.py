@@ -40,6 +40,8 @@ def test_struct_sizes_match_c_layout():
     assert C.sizeof(L.Instance) == 64
     assert C.sizeof(L.InstanceResult) == 88
     assert C.sizeof(L.ServeCompletion) == 96
+    assert C.sizeof(L.BoundedResult) == 72
+    assert C.sizeof(L.ServeConfig) == 48
 
 
 def test_status_codes_match_header():

@@ -152,6 +152,30 @@ def test_memory_bounded_mode(peng):
     assert len(mv) == r["steps"] and E.validate_puzzle_moves(4, tiles, mv)
 
 
+def test_memory_bounded_mode_exact_phase():
+    """After the table-capped segments, iterative-deepening passes (memory
+    bounded by the search depth, not by the table) reach the reference's
+    optimum and prove it: the same answer at every table cap, lower bound =
+    length.  Without the exact phase the segments' answer keeps its bound."""
+    hard = golden("mixed_c4.json")[127]  # 63 moves
+    tiles = E.gen_puzzle(hard["seed"], 4, hard["walk"])
+    opt = hard["ref"]["steps"]
+    with Engine(0, exact_ms=60000) as e:
+        e.pdb_build(4)
+        for log2 in (20, 22):
+            r = e.puzzle_solve_bounded(4, tiles, log2)
+            assert r["status"] == L.OK and r["segments"] > 1
+            assert r["exact_optimal"] == 1 and r["exact_passes"] >= 1
+            assert r["steps"] == r["lower_bound"] == opt
+            mv = e.puzzle_moves()
+            assert len(mv) == opt and E.validate_puzzle_moves(4, tiles, mv)
+    with Engine(0, exact_ms=-1) as e:
+        e.pdb_build(4)
+        r = e.puzzle_solve_bounded(4, tiles, 20)
+        assert r["status"] == L.OK and r["exact_passes"] == 0
+        assert r["lower_bound"] <= opt <= r["steps"]
+
+
 def test_pdb5_equals_reference_files(peng):
     """The four 6-tile tables of the 5x5 puzzle, byte for byte the reference's
     database_5_<tiles>.bin files (tracked order of CPU-solver.hpp:71-102)."""

@@ -28,7 +28,7 @@ class Config(C.Structure):
     _fields_ = [("heaps", C.c_int32), ("block_threads", C.c_int32), ("heap_capacity", C.c_int32),
                 ("hash_log2_slots", C.c_int32), ("max_load", C.c_double), ("max_rounds", C.c_int64),
                 ("wait_timeout_s", C.c_double), ("threads_per_heap", C.c_int32), ("heap_top_levels", C.c_int32),
-                ("dedup", C.c_int32), ("reserved", C.c_int32)]
+                ("dedup", C.c_int32), ("exact_ms", C.c_int32)]
 
 
 class GridResult(C.Structure):
@@ -48,7 +48,9 @@ class PuzzleResult(C.Structure):
 
 class BoundedResult(C.Structure):
     _fields_ = [("status", C.c_int32), ("steps", C.c_int32), ("lower_bound", C.c_int32), ("segments", C.c_int32),
-                ("expanded", C.c_int64), ("generated", C.c_int64), ("kernel_ms", C.c_double), ("solve_ms", C.c_double)]
+                ("expanded", C.c_int64), ("generated", C.c_int64), ("kernel_ms", C.c_double), ("solve_ms", C.c_double),
+                ("exact_passes", C.c_int32), ("exact_optimal", C.c_int32), ("exact_nodes", C.c_int64),
+                ("exact_ms", C.c_double)]
 
 
 class Instance(C.Structure):

@@ -1559,7 +1559,7 @@ static void serve_retire(ServeState *S, ServeTier &t, std::deque<ServeReq> &to_l
         t.descs[q].kind = 0;
         if ((status == ST_HASH_FULL || status == ST_HEAP_OVERFLOW) && r.attempts < 8) {
             if (status == ST_HASH_FULL) r.mult = std::max<uint64_t>(r.mult * (t.large ? 4 : 16), 16);
-            if (status == ST_HEAP_OVERFLOW) r.heap_mult *= t.large ? 16 : 2;
+            if (status == ST_HEAP_OVERFLOW) r.heap_mult *= t.large ? 16 : 4;
             if (large.nslots > 0) {
                 if (t.large)
                     to_large.push_front(std::move(r));
@@ -1795,7 +1795,9 @@ int32_t uastar_serve_start(uastar_engine *eng, const uastar_serve_config *cfg) {
         delete S;
         return grc;
     }
-    small.geo.set_capacity(S->cfg.heap_capacity > 0 ? (uint64_t)S->cfg.heap_capacity : 4095);
+    // resident searches keep their heaps across quanta: a request that
+    // overflows restarts, so the default leaves room (16383 entries per heap)
+    small.geo.set_capacity(S->cfg.heap_capacity > 0 ? (uint64_t)S->cfg.heap_capacity : 16383);
     large.geo = small.geo;
     large.large = true;
     const int capacity = small.geo.ctas;  // co-resident CTAs of the quantum kernels

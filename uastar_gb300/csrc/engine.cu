@@ -16,6 +16,7 @@
 #include "ga_problems.cuh"
 #include "ga_search.cuh"
 #include "ga_grow.cuh"
+#include "ga_ida.cuh"
 
 using namespace uastar;
 
@@ -666,6 +667,167 @@ void boards_to_moves(int n, const std::vector<std::vector<uint8_t>> &boards, std
     }
 }
 
+// ---- exact phase of the memory-bounded mode: IDA* passes (ga_ida.cuh) ----
+// A board on the host: tiles, blank cell, the move that reached it (+1) and
+// the moves from the start (2 bits each, first lowest).
+struct HostBoard {
+    uint8_t b[25];
+    int8_t blank;
+    uint8_t last;
+    uint64_t prefix;
+};
+
+// Blank move mv (0..3 = (+1,0), (-1,0), (0,+1), (0,-1) in (row, column), the
+// reference's DX/DY) on an n x n board; false if it leaves the board.
+template <int N> bool host_blank_move(HostBoard &h, int mv) {
+    const int bx = h.blank / N, by = h.blank % N;
+    const int nx = bx + (mv == 0) - (mv == 1), ny = by + (mv == 2) - (mv == 3);
+    if (nx < 0 || nx >= N || ny < 0 || ny >= N) return false;
+    const int q = nx * N + ny;
+    h.b[h.blank] = h.b[q];
+    h.b[q] = 0;
+    h.blank = (int8_t)q;
+    return true;
+}
+
+template <int N> bool host_is_goal(const uint8_t *b) {
+    for (int i = 0; i < N * N; ++i)
+        if (b[i] != (i + 1) % (N * N)) return false;
+    return true;
+}
+
+// The start's search tree cut at the first depth with at least `want` nodes
+// (at most max_depth <= 32), without moves that undo the previous one (the
+// search prunes those too).  A goal met on the way ends the cut: every
+// shorter move sequence was enumerated before it, so its depth is optimal.
+template <int N>
+void ida_roots(const uint8_t *tiles, size_t want, int max_depth, std::vector<IdaRoot> *roots,
+               std::vector<int32_t> *goal_moves, bool *goal) {
+    std::vector<HostBoard> cur(1), next;
+    HostBoard &s0 = cur[0];
+    std::memset(&s0, 0, sizeof s0);
+    std::memcpy(s0.b, tiles, N * N);
+    for (int i = 0; i < N * N; ++i)
+        if (!tiles[i]) s0.blank = (int8_t)i;
+    *goal = host_is_goal<N>(tiles);
+    if (*goal) return;
+    for (int d = 0; d < max_depth && cur.size() < want; ++d) {
+        next.clear();
+        next.reserve(cur.size() * 3);
+        for (const HostBoard &h : cur)
+            for (int mv = 0; mv < 4; ++mv) {
+                if (h.last && mv == ((h.last - 1) ^ 1)) continue;
+                HostBoard m = h;
+                if (!host_blank_move<N>(m, mv)) continue;
+                m.last = (uint8_t)(mv + 1);
+                m.prefix = h.prefix | ((uint64_t)mv << (2 * d));
+                if (host_is_goal<N>(m.b)) {
+                    *goal = true;
+                    goal_moves->clear();
+                    for (int j = 0; j <= d; ++j) goal_moves->push_back((int32_t)((m.prefix >> (2 * j)) & 3));
+                    return;
+                }
+                next.push_back(m);
+            }
+        cur.swap(next);
+        if (cur.size() >= want || d + 1 >= max_depth) {
+            roots->resize(cur.size());
+            for (size_t i = 0; i < cur.size(); ++i) {
+                IdaRoot &r = (*roots)[i];
+                if constexpr (N == 5) {
+                    const Key128 k = PuzzleProblem<5>::pack(cur[i].b);
+                    r.lo = k.lo;
+                    r.hi = k.hi;
+                } else {
+                    r.lo = pack_board(N, cur[i].b);
+                    r.hi = 0;
+                }
+                r.g = (uint32_t)(d + 1);
+                r.last = cur[i].last;
+                r.prefix = cur[i].prefix;
+            }
+            return;
+        }
+    }
+}
+
+// IDA* passes from the lower bound lb up to the length ub of the solution
+// in hand, for at most budget_ms.  A pass that finds a goal writes the
+// optimal moves; one that completes without a goal raises out->lower_bound
+// to its next threshold; reaching ub proves the solution in hand optimal.
+template <int N>
+int32_t ida_exact(uastar_engine *eng, const uint8_t *tiles, int32_t lb, int32_t ub, double budget_ms,
+                  std::vector<int32_t> *moves, uastar_bounded_result *out) {
+    constexpr int kMaxDepth = N == 3 ? 48 : N == 4 ? 100 : 200;
+    const double t0 = now_ms();
+    std::vector<IdaRoot> roots;
+    std::vector<int32_t> goal_moves;
+    bool goal = false;
+    ida_roots<N>(tiles, 1u << 18, 24, &roots, &goal_moves, &goal);
+    if (goal) {  // the cut met the goal first: that is the optimum
+        *moves = goal_moves;
+        out->lower_bound = (int32_t)goal_moves.size();
+        out->exact_optimal = 1;
+        out->exact_ms = now_ms() - t0;
+        return UASTAR_OK;
+    }
+    const size_t head = (sizeof(IdaPass) + 255) & ~(size_t)255;
+    cudaError_t e;
+    if ((e = eng->ida.ensure(head + roots.size() * sizeof(IdaRoot))) != cudaSuccess) return fail_cuda(eng, e, "alloc ida");
+    IdaPass *d_pass = eng->ida.as<IdaPass>();
+    IdaRoot *d_roots = reinterpret_cast<IdaRoot *>(eng->ida.as<unsigned char>() + head);
+    if ((e = cudaMemcpyAsync(d_roots, roots.data(), roots.size() * sizeof(IdaRoot), cudaMemcpyHostToDevice,
+                             eng->stream)) != cudaSuccess)
+        return fail_cuda(eng, e, "ida roots");
+    PuzzleProblem<N> prob;
+    prob.pdb = eng->pdb[N].as<uint8_t>();
+    prob.goal = PuzzleProblem<N>::goal_key();
+    prob.start = prob.goal;
+    uint32_t t = (uint32_t)std::max(lb, 0);
+    bool optimal = false;
+    while (t < (uint32_t)ub) {
+        const double left_ms = budget_ms - (now_ms() - t0);
+        if (left_ms <= 0) break;
+        IdaPass init;
+        std::memset(&init, 0, sizeof init);
+        init.min_exceed = ~0u;
+        if ((e = cudaMemcpyAsync(d_pass, &init, sizeof init, cudaMemcpyHostToDevice, eng->stream)) != cudaSuccess)
+            return fail_cuda(eng, e, "ida state");
+        // threads read the device clock at their start: the pass ends
+        // `left_ms` after it began
+        k_ida_pass<PuzzleProblem<N>, kMaxDepth><<<std::max(1, eng->sms * 8), 128, 0, eng->stream>>>(
+            prob, d_roots, (uint32_t)roots.size(), t, d_pass, (unsigned long long)(left_ms * 1e6));
+        eng->launches++;
+        if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(eng, e, "ida launch");
+        IdaPass res;
+        if ((e = cudaMemcpyAsync(&res, d_pass, sizeof res, cudaMemcpyDeviceToHost, eng->stream)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(eng->stream)) != cudaSuccess)
+            return fail_cuda(eng, e, "ida pass");
+        out->exact_passes += 1;
+        out->exact_nodes += (int64_t)res.nodes;
+        if (res.found) {
+            const IdaRoot &r = roots[res.found_root];
+            moves->clear();
+            for (uint32_t j = 0; j < r.g; ++j) moves->push_back((int32_t)((r.prefix >> (2 * j)) & 3));
+            for (uint32_t j = 0; j < res.found_len; ++j) moves->push_back((int32_t)res.moves[j]);
+            out->lower_bound = (int32_t)moves->size();
+            optimal = true;
+            break;
+        }
+        if (res.stopped) break;  // out of time (or a subtree deeper than the stack): t stays the bound
+        if (res.min_exceed == ~0u) break;  // nothing cut off and no goal: cannot happen on a solvable board
+        t = res.min_exceed;
+        out->lower_bound = std::max(out->lower_bound, (int32_t)std::min<uint32_t>(t, (uint32_t)ub));
+    }
+    if (!optimal && t >= (uint32_t)ub) {
+        out->lower_bound = ub;  // every shorter solution was ruled out
+        optimal = true;
+    }
+    out->exact_optimal = optimal ? 1 : 0;
+    out->exact_ms = now_ms() - t0;
+    return UASTAR_OK;
+}
+
 // Memory-bounded solve: segments of exact GA*, each with the table capped.
 // A segment that fills the table pauses; the open list's minimum f then is
 // a lower bound on the remaining optimum (admissible h: every optimal path
@@ -678,6 +840,20 @@ int32_t puzzle_bounded_n(uastar_engine *eng, const uint8_t *tiles, int max_log2,
     uint8_t cur[25];
     std::memcpy(cur, tiles, N * N);
     cudaError_t e;
+    // Where the segments cannot go on (their limit, or no open node to
+    // commit to), the exact phase still runs from the first bound, with no
+    // solution in hand; failing it too, the segments' status stands.
+    const auto fallback = [&](int32_t status, const char *why) -> int32_t {
+        if (eng->cfg.exact_ms >= 0) {
+            moves->clear();
+            const int32_t rc2 = ida_exact<N>(eng, tiles, out->lower_bound, 1 << 30,
+                                             eng->cfg.exact_ms > 0 ? (double)eng->cfg.exact_ms : 3000.0, moves, out);
+            if (rc2 != UASTAR_OK) return rc2;
+            if (out->exact_optimal) return UASTAR_OK;
+        }
+        eng->set_err(why);
+        return status;
+    };
     for (int seg = 0; seg < 256; ++seg) {
         PuzzleProblem<N> prob;
         prob.pdb = eng->pdb[N].as<uint8_t>();
@@ -698,6 +874,11 @@ int32_t puzzle_bounded_n(uastar_engine *eng, const uint8_t *tiles, int max_log2,
             if (seg == 0) out->lower_bound = (int32_t)po.st.goal_best;
             if ((rc = walk_boards<N>(eng, po.st.goal_slot, &boards))) return rc;
             boards_to_moves(N, boards, moves);
+            // more than one segment: the exact phase, from the first
+            // segment's bound up to this solution's length
+            if (seg > 0 && eng->cfg.exact_ms >= 0)
+                return ida_exact<N>(eng, tiles, out->lower_bound, (int32_t)moves->size(),
+                                    eng->cfg.exact_ms > 0 ? (double)eng->cfg.exact_ms : 3000.0, moves, out);
             return UASTAR_OK;
         }
         if (po.st.status != ST_RUNNING) return (int32_t)po.st.status;
@@ -712,21 +893,18 @@ int32_t puzzle_bounded_n(uastar_engine *eng, const uint8_t *tiles, int max_log2,
         cudaMemcpyAsync(&best, d_best, 8, cudaMemcpyDeviceToHost, eng->stream);
         if ((e = cudaStreamSynchronize(eng->stream)) != cudaSuccess) return fail_cuda(eng, e, "best open node");
         if (best == ~0ull) {
-            eng->set_err("bounded search: no current open node at the memory bound");
-            return UASTAR_HASH_FULL;
+            return fallback(UASTAR_HASH_FULL, "bounded search: no current open node at the memory bound");
         }
         const uint32_t f = (uint32_t)(best >> 48);  // entry key = f << 16 | (0xffff - g)
         if (seg == 0) out->lower_bound = (int32_t)f;
         if ((rc = walk_boards<N>(eng, (uint32_t)best, &boards))) return rc;
         if (boards.size() < 2) {
-            eng->set_err("bounded search: the best open node is the start");
-            return UASTAR_HASH_FULL;
+            return fallback(UASTAR_HASH_FULL, "bounded search: the best open node is the start");
         }
         boards_to_moves(N, boards, moves);
         std::memcpy(cur, boards.back().data(), N * N);
     }
-    eng->set_err("bounded search: segment limit reached");
-    return UASTAR_ITER_LIMIT;
+    return fallback(UASTAR_ITER_LIMIT, "bounded search: segment limit reached");
 }
 
 }  // namespace

@@ -85,6 +85,7 @@ struct uastar_engine {
     uastar::DevBuf tab, heaps, heap_size, cand, team, walk, bitmap;
     uastar::DevBuf tab_next, grow_map;  // table growth of a paused search
     uastar::DevBuf sortb;               // per-round successor sort (dedup = 1), uastar_sort_keys
+    uastar::DevBuf ida;                 // memory-bounded mode: IDA* roots and pass state
     // launch-configuration queries of the plain engine, made once per shape:
     // the dynamic shared memory limit set per kernel, and co-resident CTAs
     // per SM per (kernel, block, shared memory)

@@ -309,6 +309,7 @@ template <int N> struct PuzzleProblem : NarrowSlots {
         return 0;
     }
     // aux = part0 | part1 << 8 | (last move + 1) << 16
+    static constexpr uint32_t kLastMoveShift = 16;
     __device__ static uint32_t hsum(uint32_t aux) { return (aux & 0xff) + ((aux >> 8) & 0xff); }
 
     __device__ uint64_t start_key() const { return start; }
@@ -501,6 +502,8 @@ template <> struct PuzzleProblem<5> : WideSlots {
         default: return __ldg(pdb + PuzzlePatterns<5>::offset(3) + rank<3>(inv));
         }
     }
+    // aux = four 7-bit pattern parts | (last move + 1) << 28
+    static constexpr uint32_t kLastMoveShift = 28;
     __device__ static uint32_t hsum(uint32_t aux) {
         return (aux & 127u) + ((aux >> 7) & 127u) + ((aux >> 14) & 127u) + ((aux >> 21) & 127u);
     }

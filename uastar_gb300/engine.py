@@ -215,10 +215,10 @@ class Engine:
     def __init__(self, ordinal: int = 0, *, heaps: int = 0, block_threads: int = 0, heap_capacity: int = 0,
                  hash_log2_slots: int = 0, max_load: float = 0.0, max_rounds: int = 0,
                  wait_timeout_s: float = 0.0, threads_per_heap: int = 0, heap_top_levels: int = 0,
-                 dedup: int = 0):
+                 dedup: int = 0, exact_ms: int = 0):
         self._lib = L.load()
         cfg = L.Config(heaps, block_threads, heap_capacity, hash_log2_slots, max_load, max_rounds,
-                       wait_timeout_s, threads_per_heap, heap_top_levels, dedup)
+                       wait_timeout_s, threads_per_heap, heap_top_levels, dedup, exact_ms)
         self._h = self._lib.uastar_create(ordinal, C.byref(cfg))
         if not self._h:
             raise EngineError(L.CUDA_ERROR, f"cannot create an engine on CUDA device {ordinal}")
@@ -337,8 +337,10 @@ class Engine:
 
     def puzzle_solve_bounded(self, n: int, tiles: Sequence[int], max_log2_slots: int) -> dict:
         """Memory-bounded solve (dedup table capped at 2^max_log2_slots slots):
-        the returned solution's `steps`, a proven `lower_bound` on the optimum
-        and the number of exact `segments` (1: the solution is optimal)."""
+        the returned solution's `steps`, a proven `lower_bound` on the optimum,
+        the number of table-capped GA* `segments` (1: optimal) and the exact
+        IDA* phase after them (`exact_passes`, `exact_optimal`,
+        `exact_nodes`, `exact_ms`; its time is the engine's `exact_ms`)."""
         t = np.ascontiguousarray(np.asarray(tiles, dtype=np.uint8))
         r = L.BoundedResult()
         self._lib.uastar_puzzle_solve_bounded(self._h, n, _u8p(t), max_log2_slots, C.byref(r))
