@@ -152,7 +152,7 @@ template <class P> struct BrickHeap {
     static_assert(BE * sizeof(E) == 128, "one brick per 128-byte line");
     E *g;       // this heap's bricks
     E *s;       // shared top, index 0 unused
-    E *scr;     // shared scratch: two bricks
+    E *scr;     // shared scratch: three bricks (0, 1: the sift-down; 2: the buffer drain)
     uint32_t L; // levels in shared memory
 
     __device__ __forceinline__ uint32_t topn() const { return (1u << L) - 1; }
@@ -175,6 +175,24 @@ template <class P> struct BrickHeap {
         else
             P::store(g + off(i), v);
     }
+    // Root of the brick holding heap index i (i > topn), and i's depth in it.
+    __device__ __forceinline__ uint32_t brick_root(uint32_t i, uint32_t *depth = nullptr) const {
+        const uint32_t r = 31u - (uint32_t)__clz(i) - L;
+        const uint32_t d = r - (r / D) * D;
+        if (depth) *depth = d;
+        return i >> d;
+    }
+    // Start copying the brick rooted at `root` into scratch brick `h` with
+    // asynchronous global -> shared copies (no registers held); complete
+    // with cp_async_wait_all() before reading it.
+    __device__ __forceinline__ void fetch_async(uint32_t root, uint32_t h) const {
+        const char *src = reinterpret_cast<const char *>(g + off(root) - 1);
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(scr + h * BE);
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + 16u * q), "l"(src + 16 * q)
+                         : "memory");
+    }
     // Copy the brick rooted at heap index `root` into scratch half `h`.
     __device__ __forceinline__ void fetch(uint32_t root, uint32_t h) const {
         const uint4 *src = reinterpret_cast<const uint4 *>(g + off(root) - 1);
@@ -187,10 +205,13 @@ template <class P> struct BrickHeap {
     }
 };
 
-// Remove the root: returns it in `out`; `last` (the old heap[size]) is sifted
-// down from the root hole.  `size` is the size after removal.
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Fill the root hole: `last` (the old heap[size]) is sifted down from the
+// root.  `size` is the size after removal.  Returns the position where
+// `last` came to rest (every position written lies on the path to it).
 template <class P>
-__device__ __forceinline__ void heap_sift_down(const BrickHeap<P> &h, uint32_t size, typename P::Entry last) {
+__device__ __forceinline__ uint32_t heap_sift_down(const BrickHeap<P> &h, uint32_t size, typename P::Entry last) {
     using E = typename P::Entry;
     constexpr uint32_t D = BrickHeap<P>::D, BE = BrickHeap<P>::BE;
     const uint32_t topn = h.topn();
@@ -209,14 +230,14 @@ __device__ __forceinline__ void heap_sift_down(const BrickHeap<P> &h, uint32_t s
         }
         if (!P::less(a, last)) {
             h.s[now] = last;
-            return;
+            return now;
         }
         h.s[now] = a;
         now = c;
     }
     if ((now << 1) > size) {
         h.st(now, last);
-        return;
+        return now;
     }
     // global bricks: `half` is the scratch half holding the brick of `now`
     // (none while `now` is in shared memory), `depth` its level in that brick
@@ -254,6 +275,7 @@ __device__ __forceinline__ void heap_sift_down(const BrickHeap<P> &h, uint32_t s
         now = c + (right ? 1u : 0u);
     }
     h.st(now, last);
+    return now;
 }
 
 // Fill the vacant heap position `now` with v, moving v up as far as it goes.
@@ -323,7 +345,8 @@ __device__ __forceinline__ void heap_push(const BrickHeap<P> &h, uint32_t &size,
 // Insert the n entries at v (an insertion buffer's drain).  They take the
 // positions size+1 .. size+n, consecutive leaves at the bottom of the tree
 // that share one brick (two at a brick or level boundary): that brick is
-// read once into scratch half 1, every entry's climb inside it runs there,
+// read once into scratch brick 2 (`have`: already there, read ahead by the
+// caller), every entry's climb inside it runs there,
 // and it is written back when the bottom moves to another brick, before a
 // climb that leaves it (finished by heap_climb from the brick above), and at
 // the end.  A drain of n entries so waits on global memory about once
@@ -331,12 +354,12 @@ __device__ __forceinline__ void heap_push(const BrickHeap<P> &h, uint32_t &size,
 // read: nothing else in that brick is in use.)
 template <class P>
 __device__ __forceinline__ void heap_push_run(const BrickHeap<P> &h, uint32_t &size, const typename P::Entry *v,
-                                              uint32_t n) {
+                                              uint32_t n, uint32_t have = 0) {
     using E = typename P::Entry;
     constexpr uint32_t D = BrickHeap<P>::D, BE = BrickHeap<P>::BE;
     const uint32_t topn = h.topn();
-    E *const b = h.scr + BE;  // scratch half 1
-    uint32_t cached = 0;      // root of the brick held in b (0: none)
+    E *const b = h.scr + 2 * BE;  // scratch brick 2
+    uint32_t cached = have;       // root of the brick held in b (0: none)
     const auto flush = [&]() {
         if (!cached) return;
         uint4 *const gl = reinterpret_cast<uint4 *>(h.g + h.off(cached) - 1);
@@ -359,7 +382,7 @@ __device__ __forceinline__ void heap_push_run(const BrickHeap<P> &h, uint32_t &s
         const uint32_t root = now >> d;
         if (root != cached) {
             flush();
-            if (d > 0) h.fetch(root, 1);
+            if (d > 0) h.fetch(root, 2);
             cached = root;
         }
         uint32_t loc = (1u << d) | (now & ((1u << d) - 1u));
@@ -602,7 +625,7 @@ template <class P> struct SearchSmem {
         return (tops_offset(H) + (size_t)H * (1u << L) * sizeof(E) + 127) & ~(size_t)127;
     }
     static __host__ __device__ size_t buf_offset(uint32_t H, uint32_t L) {
-        return scr_offset(H, L) + (size_t)H * 2 * 128;
+        return scr_offset(H, L) + (size_t)H * 3 * 128;
     }
     static __host__ __device__ size_t scratch_offset(uint32_t H, uint32_t L) {
         return buf_offset(H, L) + (size_t)H * kBuf * sizeof(E);
@@ -690,7 +713,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
 
     E *const gblock = m.heaps + (size_t)(owner ? myh : 0) * m.stride;  // saved top, then bricks
     BrickHeap<P> myheap{gblock + top_reserve<P>(L), tops + (size_t)(owner ? tid : 0) * (1u << L),
-                        scr + (size_t)(owner ? tid : 0) * 2 * BrickHeap<P>::BE, L};
+                        scr + (size_t)(owner ? tid : 0) * 3 * BrickHeap<P>::BE, L};
     // The heap's insertion buffer: an unordered list of up to kBuf entries in
     // shared memory in front of the heap.  The push phase only appends to it;
     // a pop takes the smaller of the heap's root and the buffer's minimum;
@@ -856,15 +879,34 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         // root hole, then drain the insertion buffer down to kBuf - kMoves
         // entries (room for this round's pushes).
         const auto chores = [&]() {
-            if (pending_sift) heap_sift_down<P>(myheap, hs, last);
-            if (bn > kBuf - P::kMoves) {
-                // move the buffer's largest entries (the small ones are
-                // popped soon) to its end, then push them as one run
-                uint32_t run = bn - (kBuf - P::kMoves);
-                if (hs + run > m.hcap) {
-                    set_error(&st->err[r3], ST_HEAP_OVERFLOW);  // this round's decision stops the search
-                    run = m.hcap > hs ? m.hcap - hs : 0u;
+            // the buffer's run to drain (its largest entries: the small ones
+            // are popped soon), down to room for this round's pushes
+            uint32_t run = bn > kBuf - P::kMoves ? bn - (kBuf - P::kMoves) : 0u;
+            if (hs + run > m.hcap) {
+                set_error(&st->err[r3], ST_HEAP_OVERFLOW);  // this round's decision stops the search
+                run = m.hcap > hs ? m.hcap - hs : 0u;
+            }
+            // the run's bottom brick is read while the sift-down runs (a
+            // fresh bottom brick, at depth 0, needs no read)
+            uint32_t pre = 0;
+            if (run && hs + 1 > topn) {
+                uint32_t d;
+                const uint32_t root = myheap.brick_root(hs + 1, &d);
+                if (d > 0) {
+                    myheap.fetch_async(root, 2);
+                    pre = root;
                 }
+            }
+            if (pending_sift) {
+                const uint32_t fin = heap_sift_down<P>(myheap, hs, last);
+                // the sift wrote into that brick: its copy is stale
+                if (pre && fin > topn && myheap.brick_root(fin) == pre) {
+                    cp_async_wait_all();
+                    pre = 0;
+                }
+            }
+            if (pre) cp_async_wait_all();
+            if (run) {
                 for (uint32_t q = 0; q < run; ++q) {
                     const uint32_t end = bn - 1 - q;
                     uint32_t bx = 0;
@@ -874,7 +916,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                     ibuf[bx] = ibuf[end];
                     ibuf[end] = e;
                 }
-                heap_push_run<P>(myheap, hs, ibuf + (bn - run), run);
+                heap_push_run<P>(myheap, hs, ibuf + (bn - run), run, pre);
                 bn -= run;
             }
         };
