@@ -544,6 +544,19 @@ def section_c5(eng, args):
                  if i < len(stream))
         out["optimal_agreement"] = f"{ok}/{sum(1 for i in gold if i < len(stream))}"
         out["optimal_sample"] = "seeded sample of the stream with its 64 largest grids and 64 longest walks"
+    # every served result against the batched engine on the same requests
+    # (another scheduling of the same search kernels), in chunks
+    t0 = time.perf_counter()
+    agree_b = 0
+    for c0 in range(0, len(stream), args.check_chunk):
+        part = stream[c0:c0 + args.check_chunk]
+        insts = WL.parallel_map(lambda x: x[1].instance(), part)
+        res, _ = eng.batch_solve(insts)
+        agree_b += sum(int(same_result(spec, served.get(c0 + k), r)) for k, ((_, spec), r) in enumerate(zip(part, res))
+                       if r["status"] == 0)
+        del insts
+    out["batched_compared"] = f"{agree_b}/{len(stream)} served results equal the batched engine's " \
+                              f"({time.perf_counter() - t0:.0f} s)"
     # the plain engine, one request at a time, in stream order, under a time guard
     t0 = time.perf_counter()
     n = agree = 0
@@ -838,6 +851,7 @@ def main():
     ap.add_argument("--serve-timeout", type=float, default=600.0)
     ap.add_argument("--plain-budget", type=float, default=420.0,
                     help="seconds of plain-engine solves over the serving stream")
+    ap.add_argument("--check-chunk", type=int, default=2500, help="serving: requests per batched check call")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--tune-stride", type=int, default=4)
     ap.add_argument("--cpu-sections", type=int, default=1, help="CPU baselines of the c3/c4/c5 sections")
