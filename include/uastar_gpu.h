@@ -312,7 +312,8 @@ typedef struct {
     int32_t slots;            /* max concurrently resident requests (0 -> all CTAs) */
     int32_t threads_per_instance;
     int32_t threads_per_heap;
-    int32_t heap_capacity;    /* entries per heap of a CTA slot (0 -> 16383; 4x on overflow) */
+    int32_t heap_capacity;    /* entries per heap of a CTA slot (0 -> 16383, 4095 where the budget's
+                                 heap share cannot hold one slot of those; 4x on overflow) */
     int32_t rounds_per_quantum; /* cap on GA* rounds per persistent-kernel launch (0 -> 65536 with
                                    a time slice, 256 without) */
     double load_factor;

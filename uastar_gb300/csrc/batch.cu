@@ -1823,6 +1823,11 @@ int32_t uastar_serve_start(uastar_engine *eng, const uastar_serve_config *cfg) {
     const uint64_t bm_words = (uint64_t)(budget_b * 0.05 / 8);
     const double tab_b = budget_b * 0.75;
     S->heap_bytes = heap_units * 16;
+    if (S->cfg.heap_capacity <= 0 && heap_units * 16 < (uint64_t)small.geo.H * small.geo.slice) {
+        // a small budget: the default heaps shrink to what one slot's share allows
+        small.geo.set_capacity(4095);
+        large.geo.set_capacity(4095);
+    }
     if (tab_b < (double)(1u << 20) * sizeof(Slot) || heap_units * 16 < (uint64_t)small.geo.H * small.geo.slice) {
         delete S;
         eng->set_err("serving budget too small");
