@@ -418,7 +418,8 @@ def section_c4(eng, args):
         tune = {"sample": f"every {args.tune_stride}th instance ({len(insts[::args.tune_stride])})",
                 "seconds": round(time.perf_counter() - t0, 2), "configs_timed": cfg.get("tried"),
                 "chosen": {k: cfg[k] for k in ("threads_per_instance", "threads_per_heap", "heap_capacity",
-                                               "load_factor", "cluster_size", "tier1_rounds")}}
+                                               "load_factor", "cluster_size", "tier1_rounds",
+                                               "tier2_puzzle_rounds")}}
     kw = {k: cfg.get(k, 0) for k in ("threads_per_instance", "threads_per_heap", "heap_capacity", "load_factor",
                                      "cluster_size", "tier1_rounds", "tier2_puzzle_rounds")}
     res, st = eng.batch_solve(insts, **kw)  # warm-up (allocations, graph)
@@ -853,7 +854,7 @@ def main():
                     help="seconds of plain-engine solves over the serving stream")
     ap.add_argument("--check-chunk", type=int, default=2500, help="serving: requests per batched check call")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--tune-stride", type=int, default=4)
+    ap.add_argument("--tune-stride", type=int, default=2)
     ap.add_argument("--cpu-sections", type=int, default=1, help="CPU baselines of the c3/c4/c5 sections")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds per section CPU baseline")
     ap.add_argument("--cpu-solve-cap", type=int, default=4_000_000, help="expansions per CPU baseline solve")

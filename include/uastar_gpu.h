@@ -298,8 +298,9 @@ int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int
  * sample of it: one pass of coordinate descent from the defaults over
  * threads_per_instance {128, 256, 512}, threads_per_heap {2, 4, 8} (heaps per
  * instance = their quotient), heap_capacity {1023, 4095, 16383},
- * load_factor {0.35, 0.5, 0.7}, cluster_size {4, 8, 16} and tier1_rounds
- * {1024, 2048, 4096}, each knob taking the value of least wall time with
+ * load_factor {0.35, 0.5, 0.7}, cluster_size {4, 8, 16}, tier1_rounds
+ * {1024, 2048, 4096} and tier2_puzzle_rounds {4096, 16384, 65536}, each knob
+ * taking the value of least wall time with
  * the others held.  Writes the choice; best->reserved = configurations timed.
  * Replaces the reference's compile-time sizes (src/pathway/GPU-solver.hpp:6-17,
  * src/puzzle/GPU-solver.cuh:11-20). */

@@ -935,8 +935,8 @@ int32_t uastar_autotune(uastar_engine *eng, const uastar_instance *sample, int32
     // defaults, each knob in turn takes the value that solves the sample in
     // the least wall time with the others held.  Knobs: CTA size per
     // instance, threads per heap (together: heaps per instance), entries per
-    // heap, dedup-partition load factor, CTAs per cluster team and the
-    // single-CTA tier's round budget.
+    // heap, dedup-partition load factor, CTAs per cluster team, the
+    // single-CTA tier's round budget and the cluster tier's puzzle budget.
     struct Knob {
         int32_t uastar_batch_config::*i;
         double uastar_batch_config::*d;
@@ -949,6 +949,7 @@ int32_t uastar_autotune(uastar_engine *eng, const uastar_instance *sample, int32
         {nullptr, &uastar_batch_config::load_factor, {0.35, 0.5, 0.7}},
         {&uastar_batch_config::cluster_size, nullptr, {4, 8, 16}},
         {&uastar_batch_config::tier1_rounds, nullptr, {1024, 2048, 4096}},
+        {&uastar_batch_config::tier2_puzzle_rounds, nullptr, {4096, 16384, 65536}},
     };
     uastar_batch_config cur{};
     cur.threads_per_instance = 256;
@@ -957,6 +958,7 @@ int32_t uastar_autotune(uastar_engine *eng, const uastar_instance *sample, int32
     cur.load_factor = 0.5;
     cur.cluster_size = 8;
     cur.tier1_rounds = 2048;
+    cur.tier2_puzzle_rounds = 16384;
     cur.use_graph = 1;
     std::vector<uastar_instance_result> res(count);
     auto time_of = [&](const uastar_batch_config &c) -> double {
