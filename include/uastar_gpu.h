@@ -311,8 +311,9 @@ int32_t uastar_autotune(uastar_engine *eng, const uastar_instance *sample, int32
 typedef struct {
     double hbm_budget_gb;     /* admission budget for heaps + dedup partitions (default 120) */
     int32_t slots;            /* max concurrently resident requests (0 -> all CTAs) */
-    int32_t threads_per_instance;
-    int32_t threads_per_heap;
+    int32_t threads_per_instance; /* threads of a CTA slot (0 -> 256) */
+    int32_t threads_per_heap; /* 0 -> 2: 128 heaps per CTA slot (a resident search's rounds are
+                                 its latency; more pops per round shorten it) */
     int32_t heap_capacity;    /* entries per heap of a CTA slot (0 -> 16383, 4095 where the budget's
                                  heap share cannot hold one slot of those; 4x on overflow) */
     int32_t rounds_per_quantum; /* cap on GA* rounds per persistent-kernel launch (0 -> 65536 with
@@ -323,7 +324,7 @@ typedef struct {
     int32_t quantum_us;       /* time slice of a persistent-kernel launch: every resident search
                                  runs rounds until this many microseconds have passed since the
                                  launch began, so that fast and slow searches share the GPU's time
-                                 rather than a round count (0 -> 4000; < 0 -> none, rounds only) */
+                                 rather than a round count (0 -> 8000; < 0 -> none, rounds only) */
 } uastar_serve_config;
 
 typedef struct {

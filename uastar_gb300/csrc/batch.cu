@@ -1260,9 +1260,13 @@ static BatchArgs serve_args(ServeState *S, ServeTier &t) {
     a.L_grid = t.geo.L_grid;
     a.L_puzzle = t.geo.L_puzzle;
     // a time slice per launch (every resident search runs until it has
-    // passed), capped by a round count; or, without a slice, the round count
+    // passed), capped by a round count; or, without a slice, the round count.
+    // 8 ms by default: the first 4000 requests of the 20000-request stream at
+    // 1000/s served at 193 / 225 / 231-257 / 252 / 250 solves/s with 2 / 4 /
+    // 8 / 12 / 16 ms slices (a launch's fixed costs against the wait of a
+    // finished request for its slice's end).
     const bool sliced = S->cfg.quantum_us >= 0;
-    a.quantum_ns = sliced ? (uint64_t)(S->cfg.quantum_us > 0 ? S->cfg.quantum_us : 4000) * 1000ull : 0;
+    a.quantum_ns = sliced ? (uint64_t)(S->cfg.quantum_us > 0 ? S->cfg.quantum_us : 8000) * 1000ull : 0;
     a.budget = (uint64_t)(S->cfg.rounds_per_quantum > 0 ? S->cfg.rounds_per_quantum : sliced ? 65536 : 256);
     a.serving = 1;
     a.keys = t.d_keys.as<unsigned long long>();
@@ -1792,7 +1796,12 @@ int32_t uastar_serve_start(uastar_engine *eng, const uastar_serve_config *cfg) {
     if (cfg) S->cfg = *cfg;
     if (!(S->cfg.hbm_budget_gb > 0)) S->cfg.hbm_budget_gb = 120.0;
     ServeTier &small = S->tier[0], &large = S->tier[1];
-    int32_t grc = resolve_block_geometry(eng, S->cfg.threads_per_instance, S->cfg.threads_per_heap, &small.geo);
+    // Two threads per heap: a resident search's latency is its rounds, and
+    // 128 heaps per CTA pop twice as many entries per round as 64 (the
+    // 20000-request stream's first 4000 at 1000/s: 219-227 solves/s against
+    // 154 with 4 threads per heap, 175-186 with 1).
+    const int tph = S->cfg.threads_per_heap > 0 ? S->cfg.threads_per_heap : 2;
+    int32_t grc = resolve_block_geometry(eng, S->cfg.threads_per_instance, tph, &small.geo);
     if (grc) {
         delete S;
         return grc;

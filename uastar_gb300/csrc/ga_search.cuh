@@ -278,28 +278,46 @@ __device__ __forceinline__ uint32_t heap_sift_down(const BrickHeap<P> &h, uint32
     return now;
 }
 
+// Entry at heap index `par` (the parent of a brick's root), from the shared
+// top or else by reading its whole brick into scratch half `half`: the brick
+// a climb that passes `par` continues in, so that it is read only once.
+template <class P>
+__device__ __forceinline__ typename P::Entry heap_parent(const BrickHeap<P> &h, uint32_t par, uint32_t half) {
+    constexpr uint32_t BE = BrickHeap<P>::BE;
+    if (par <= h.topn()) return h.s[par];
+    uint32_t d;
+    const uint32_t root = h.brick_root(par, &d);
+    h.fetch(root, half);
+    return h.scr[half * BE + ((1u << d) | (par & ((1u << d) - 1u)))];
+}
+
 // Fill the vacant heap position `now` with v, moving v up as far as it goes.
 // Below the shared top the climb works brick by brick: the brick holding the
-// current position is read once (one burst of independent loads) into
-// scratch half 0, the climb inside it runs in shared memory and the brick is
-// written back, so a climb waits on global memory once per brick it passes
-// through (most pass none or one) instead of once per level.  `bottom`: `now`
-// is the heap's new last position, so a brick rooted there holds nothing
-// else yet (all its other positions are below it) and is not read.
+// current position is read once (one burst of independent loads) into a
+// scratch half, the climb inside it runs in shared memory and the brick is
+// written back; at a brick's root the parent's whole brick is read into the
+// other half, which the climb continues in if it goes on, so a climb waits
+// on global memory once per brick it passes through (most pass none or one)
+// instead of once per level.  `bottom`: `now` is the heap's new last
+// position, so a brick rooted there holds nothing else yet (all its other
+// positions are below it) and is not read.  `have` >= 0: the brick of `now`
+// is already in that scratch half.
 template <class P>
 __device__ __forceinline__ void heap_climb(const BrickHeap<P> &h, uint32_t now, const typename P::Entry &v,
-                                           bool bottom = false) {
+                                           bool bottom = false, int have = -1) {
     using E = typename P::Entry;
-    constexpr uint32_t D = BrickHeap<P>::D;
+    constexpr uint32_t BE = BrickHeap<P>::BE;
     const uint32_t topn = h.topn();
+    int cur = have;
     while (now > topn) {
-        const uint32_t l = 31u - (uint32_t)__clz(now);
-        const uint32_t r = l - h.L;
-        const uint32_t d = r - (r / D) * D;  // depth of `now` in its brick
-        const uint32_t root = now >> d;
-        if (!(bottom && d == 0)) h.fetch(root, 0);
+        uint32_t d;
+        const uint32_t root = h.brick_root(now, &d);  // d = depth of `now` in its brick
+        if (cur < 0) {
+            if (!(bottom && d == 0)) h.fetch(root, 0);
+            cur = 0;
+        }
         bottom = false;
-        E *const b = h.scr;
+        E *const b = h.scr + cur * BE;
         uint4 *const gl = reinterpret_cast<uint4 *>(h.g + h.off(root) - 1);
         uint32_t loc = (1u << d) | (now & ((1u << d) - 1u));
         while (loc > 1) {
@@ -311,8 +329,9 @@ __device__ __forceinline__ void heap_climb(const BrickHeap<P> &h, uint32_t now, 
         }
         bool done = loc > 1;
         if (!done) {
-            // at the brick's root: its parent is in the brick above or the shared top
-            const E pv = h.ld(now >> 1);
+            // at the brick's root: its parent is in the brick above (read
+            // into the other half) or in the shared top
+            const E pv = heap_parent<P>(h, now >> 1, (uint32_t)(cur ^ 1));
             if (!P::less(v, pv)) {
                 done = true;
             } else {
@@ -325,6 +344,7 @@ __device__ __forceinline__ void heap_climb(const BrickHeap<P> &h, uint32_t now, 
 #pragma unroll
         for (int q = 0; q < 8; ++q) gl[q] = src[q];
         if (done) return;
+        cur ^= 1;  // the parent's brick, if `now` is still below the top
     }
     while (now > 1) {
         const uint32_t par = now >> 1;
@@ -397,16 +417,16 @@ __device__ __forceinline__ void heap_push_run(const BrickHeap<P> &h, uint32_t &s
             b[loc] = x;
             continue;
         }
-        // at the brick's root: its parent is in the brick above or the shared
-        // top, neither of which is cached
-        const E pv = h.ld(now >> 1);
+        // at the brick's root: its parent is in the brick above (read whole
+        // into scratch half 0, where the climb continues) or the shared top
+        const E pv = heap_parent<P>(h, now >> 1, 0);
         if (!P::less(x, pv)) {
             b[1] = x;
             continue;
         }
         b[1] = pv;
         flush();
-        heap_climb<P>(h, now >> 1, x);
+        heap_climb<P>(h, now >> 1, x, false, 0);
     }
     flush();
 }
@@ -617,18 +637,29 @@ template <class P> struct SearchSmem {
     using E = typename P::Entry;
     // entries of a heap's insertion buffer: two rounds of pushes
     static constexpr uint32_t kBuf = 2 * P::kMoves;
+    // Per-heap strides (entries) of the heap tops, brick scratch and
+    // insertion buffers.  Heap h's owner is lane h % 32 of an owner warp, and
+    // the owners walk their heaps in step: unpadded, every stride is a
+    // multiple of 128 bytes, so all lanes of a warp would hit the same banks
+    // (a 16- or 32-way conflict on every access).  One extra entry (16 bytes
+    // for the scratch, whose bricks are copied with 16-byte cp.async) moves
+    // consecutive heaps two or four banks apart: an 8-byte access of a half
+    // warp and a 16-byte access of a quarter warp touch distinct banks.
+    static __host__ __device__ constexpr uint32_t top_stride(uint32_t L) { return (1u << L) + 1u; }
+    static constexpr uint32_t kScrStride = 3 * BrickHeap<P>::BE + 16 / sizeof(E);
+    static constexpr uint32_t kBufStride = kBuf + 1;
     // pops, heap tops, brick scratch, insertion buffers, then warp totals
     static __host__ __device__ size_t tops_offset(uint32_t H) {
         return ((size_t)H * sizeof(PopInfo<typename P::Key>) + 15) & ~(size_t)15;
     }
     static __host__ __device__ size_t scr_offset(uint32_t H, uint32_t L) {
-        return (tops_offset(H) + (size_t)H * (1u << L) * sizeof(E) + 127) & ~(size_t)127;
+        return (tops_offset(H) + (size_t)H * top_stride(L) * sizeof(E) + 127) & ~(size_t)127;
     }
     static __host__ __device__ size_t buf_offset(uint32_t H, uint32_t L) {
-        return scr_offset(H, L) + (size_t)H * 3 * 128;
+        return scr_offset(H, L) + (size_t)H * kScrStride * sizeof(E);
     }
     static __host__ __device__ size_t scratch_offset(uint32_t H, uint32_t L) {
-        return buf_offset(H, L) + (size_t)H * kBuf * sizeof(E);
+        return (buf_offset(H, L) + (size_t)H * kBufStride * sizeof(E) + 15) & ~(size_t)15;
     }
     // warp totals of the block scans, this CTA's round counters, then the
     // owner warps' minimum popped f (16 x 8 bytes)
@@ -712,8 +743,8 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
     uint32_t *scratch = reinterpret_cast<uint32_t *>(smem + SearchSmem<P>::scratch_offset(H, L));
 
     E *const gblock = m.heaps + (size_t)(owner ? myh : 0) * m.stride;  // saved top, then bricks
-    BrickHeap<P> myheap{gblock + top_reserve<P>(L), tops + (size_t)(owner ? tid : 0) * (1u << L),
-                        scr + (size_t)(owner ? tid : 0) * 3 * BrickHeap<P>::BE, L};
+    BrickHeap<P> myheap{gblock + top_reserve<P>(L), tops + (size_t)(owner ? tid : 0) * SearchSmem<P>::top_stride(L),
+                        scr + (size_t)(owner ? tid : 0) * SearchSmem<P>::kScrStride, L};
     // The heap's insertion buffer: an unordered list of up to kBuf entries in
     // shared memory in front of the heap.  The push phase only appends to it;
     // a pop takes the smaller of the heap's root and the buffer's minimum;
@@ -721,7 +752,8 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
     // phase (drain), off the round's critical path, keeping room for the next
     // push phase.  The heap and the buffer together are the priority queue.
     constexpr uint32_t kBuf = SearchSmem<P>::kBuf;
-    E *const ibuf = reinterpret_cast<E *>(smem + SearchSmem<P>::buf_offset(H, L)) + (size_t)(owner ? tid : 0) * kBuf;
+    E *const ibuf =
+        reinterpret_cast<E *>(smem + SearchSmem<P>::buf_offset(H, L)) + (size_t)(owner ? tid : 0) * SearchSmem<P>::kBufStride;
     uint32_t bn = 0;  // entries in ibuf (owner; empty whenever the search is parked)
     uint64_t nE = 0, nS = 0, nP = 0;
 
