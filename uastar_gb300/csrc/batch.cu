@@ -77,6 +77,7 @@ struct BatchArgs {
     uint32_t L_grid, L_puzzle;            // heap levels in shared memory
     uint32_t stride_grid, stride_puzzle;  // batch heap geometry per entry type
     uint32_t hcap_grid, hcap_puzzle;
+    uint32_t split_grid, split_puzzle;    // SearchMem::split per entry type
     InstOut *outs;
     TeamState *states;     // serving: per slot persisted team state
     TeamState *cstates;    // cluster teams: per cluster team state
@@ -136,6 +137,7 @@ __device__ uint32_t run_instance(const BatchArgs &a, const InstDesc &d, Team &te
                                a.L_grid, hs, cand, d.max_rounds};
         if (d.grow_at) m.grow_at = d.grow_at;
         m.deadline_ns = deadline_ns;
+        m.split = a.split_grid;
         return ga_search(prob, team, m, a.H, smem, budget);
     }
     SearchMem<PuzzleEntry> m{tab, slots - 1, (uint64_t)(slots * a.max_load), 4096u,
@@ -144,6 +146,7 @@ __device__ uint32_t run_instance(const BatchArgs &a, const InstDesc &d, Team &te
                              a.L_puzzle, hs, cand, d.max_rounds};
     if (d.grow_at) m.grow_at = d.grow_at;
     m.deadline_ns = deadline_ns;
+    m.split = a.split_puzzle;
     if (d.n == 4) {
         PuzzleProblem<4> prob;
         prob.pdb = a.pdb4;
@@ -417,6 +420,10 @@ struct BatchGeometry {
     HeapGeometry<PuzzleProblem<4>> hg_puzzle;
     uint64_t slice;  // bytes per heap
     size_t smem;
+    // Split rounds (SearchMem::split) where their push staging fits the
+    // shared memory the CTA already has: the puzzles' tops are the smaller,
+    // so puzzles get them at every launch shape here, grids not.
+    uint32_t split_grid = 0, split_puzzle = 0;
     double load;
     void set_capacity(uint64_t w) {
         want = w;
@@ -451,6 +458,8 @@ int32_t resolve_block_geometry(uastar_engine *eng, int threads, int tph, BatchGe
     g->L_puzzle = fit_top<PuzzleProblem<4>>(g->H, per_cta);
     g->smem = std::max(SearchSmem<GridProblem>::bytes(g->H, g->L_grid),
                        SearchSmem<PuzzleProblem<4>>::bytes(g->H, g->L_puzzle));
+    g->split_grid = SearchSmem<GridProblem>::bytes_split(g->H, g->L_grid) <= g->smem ? 1u : 0u;
+    g->split_puzzle = SearchSmem<PuzzleProblem<4>>::bytes_split(g->H, g->L_puzzle) <= g->smem ? 1u : 0u;
     g->set_capacity(4095);
     cudaError_t e = cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g->smem);
     if (e != cudaSuccess) return fail_cuda(eng, e, "smem attribute");
@@ -612,6 +621,8 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
     a.stride_puzzle = g.hg_puzzle.stride;
     a.hcap_grid = g.hg_grid.hcap;
     a.hcap_puzzle = g.hg_puzzle.hcap;
+    a.split_grid = g.split_grid;
+    a.split_puzzle = g.split_puzzle;
     a.budget = budget;
     a.region_slots = region_slots;
     a.keys = eng->b_walk.as<unsigned long long>();
@@ -1259,6 +1270,8 @@ static BatchArgs serve_args(ServeState *S, ServeTier &t) {
     a.H = t.geo.H;
     a.L_grid = t.geo.L_grid;
     a.L_puzzle = t.geo.L_puzzle;
+    a.split_grid = t.geo.split_grid;
+    a.split_puzzle = t.geo.split_puzzle;
     // a time slice per launch (every resident search runs until it has
     // passed), capped by a round count; or, without a slice, the round count.
     // 8 ms by default: the first 4000 requests of the 20000-request stream at

@@ -78,6 +78,13 @@ template <class E> struct SearchMem {
     // 0 = none.  The serving loop's quanta end on it, so that every resident
     // search runs for the same time rather than the same number of rounds.
     uint64_t deadline_ns = 0;
+    // Split rounds (CTA and cluster teams, table-minimum dedup, separate
+    // owner warps): the heap owners arrive at the team barrier as soon as
+    // their pops are published and refill their heaps while the relaxers
+    // finish, pass the barrier, decide and stage the pushes; the owners then
+    // wait for the staging only.  Needs SearchSmem<P>::bytes_split shared
+    // memory.  0 = one barrier for all threads.
+    uint32_t split = 0;
     // Sort-based dedup (ga_search<.., true>): every round's successors are
     // radix-sorted by key and each key's minimum-g record is relaxed once.
     unsigned long long *sort_buf = nullptr;  // 2 x C * H * kMoves pairs
@@ -85,8 +92,29 @@ template <class E> struct SearchMem {
     uint32_t sort_bits = 0;                  // key bits to sort on
 };
 
+// Named CTA barriers (0 is __syncthreads): barrier.sync waits for `n`
+// threads (a multiple of 32) to have arrived; barrier.arrive counts this
+// thread without waiting.  Both order this thread's earlier memory accesses
+// before the barrier's completion for the threads that wait on it.  The
+// non-.aligned forms: a warp may reach them diverged (owner lanes leave
+// their chores at different times).
+__device__ __forceinline__ void named_sync(uint32_t id, uint32_t n) {
+    asm volatile("barrier.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+__device__ __forceinline__ void named_arrive(uint32_t id, uint32_t n) {
+    asm volatile("barrier.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
 // ------------------------------------------------------------------ teams ---
+// Split rounds (SearchMem::split) need the team barrier in two halves:
+// early_arrive() by the owner warps (no wait), relaxers_sync() by the
+// relaxer warps (arrive and wait), late_wait() by the owner warps after
+// their chores.  The grid team has no split form.
 struct GridTeam {
+    static constexpr bool kSplit = false;
+    __device__ void early_arrive() {}  // (no split form: never called)
+    __device__ void relaxers_sync(uint32_t) {}
+    __device__ void late_wait() {}
     TeamState *st;  // global memory
     uint32_t epoch;
     uint64_t timeout_ns;
@@ -104,6 +132,7 @@ struct GridTeam {
 // cluster scope orders every memory access of the cluster's threads, global
 // ones included, so no separate fence is needed.
 struct ClusterTeam {
+    static constexpr bool kSplit = true;
     TeamState *st;  // global memory
     __device__ uint32_t cta() const {
         uint32_t r;
@@ -118,15 +147,27 @@ struct ClusterTeam {
     __device__ void sync() {
         asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
     }
+    // split halves: the cluster barrier's own arrive and wait, in the forms
+    // that a diverged warp may execute
+    __device__ void early_arrive() { asm volatile("barrier.cluster.arrive.release;" ::: "memory"); }
+    __device__ void relaxers_sync(uint32_t) {
+        asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+    }
+    __device__ void late_wait() { asm volatile("barrier.cluster.wait.acquire;" ::: "memory"); }
     __device__ uint64_t rd64(const unsigned long long *p) const { return ldcg_u64(p); }
     __device__ uint32_t rd32(const uint32_t *p) const { return ldcg_u32(p); }
 };
 
 struct BlockTeam {
+    static constexpr bool kSplit = true;
     TeamState *st;  // shared memory
     __device__ uint32_t cta() const { return 0; }
     __device__ uint32_t ctas() const { return 1; }
     __device__ void sync() { __syncthreads(); }
+    // split halves: named barrier 1 over the whole CTA, owners arriving early
+    __device__ void early_arrive() { named_arrive(1, blockDim.x); }
+    __device__ void relaxers_sync(uint32_t n) { named_sync(1, n); }
+    __device__ void late_wait() {}
     __device__ uint64_t rd64(const unsigned long long *p) const {
         return *reinterpret_cast<const volatile unsigned long long *>(p);
     }
@@ -667,8 +708,12 @@ template <class P> struct SearchSmem {
     static __host__ __device__ size_t bytes(uint32_t H, uint32_t L) {
         return scratch_offset(H, L) + 4 * kScratchWords;
     }
-    // the sort-based dedup's shared memory follows (T threads per CTA)
+    // the sort-based dedup's shared memory follows (T threads per CTA); or,
+    // with split rounds, the push staging (the sift scratch is busy then)
     static __host__ __device__ size_t sort_offset(uint32_t H, uint32_t L) { return (bytes(H, L) + 15) & ~(size_t)15; }
+    static __host__ __device__ size_t bytes_split(uint32_t H, uint32_t L) {
+        return sort_offset(H, L) + (size_t)H * P::kMoves * sizeof(E);
+    }
     static __host__ __device__ size_t bytes_sorted(uint32_t H, uint32_t L, uint32_t T) {
         return sort_offset(H, L) + sort_smem_bytes(T);
     }
@@ -735,6 +780,9 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
     const uint32_t rfirst = T > owner_warps * 32u ? owner_warps * 32u : 0u;
     const uint32_t rthreads = T - rfirst;
     const bool relaxer = tid >= rfirst;
+    // split rounds (SearchMem::split), uniform over the team
+    bool split = false;
+    if constexpr (Team::kSplit && !kSort) split = m.split != 0 && rfirst > 0;
 
     using Key = typename P::Key;
     PopInfo<Key> *pop = reinterpret_cast<PopInfo<Key> *>(smem);
@@ -805,7 +853,11 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
     // H * kMoves), then the C + 1 region offsets of the round's candidates
     // (the host keeps C < 32 H); it reuses the sift-down scratch, idle then.
     static_assert(2 * BrickHeap<P>::BE >= P::kMoves, "staging fits the sift scratch");
-    E *const stage = scr;
+    // With split rounds the owners may still be sifting while the relaxers
+    // stage, so the staging has its own room after the CTA's other shared
+    // memory (bytes_split).
+    E *const stage =
+        split ? reinterpret_cast<E *>(smem + SearchSmem<P>::sort_offset(H, L)) : scr;
     uint32_t *const roff = reinterpret_cast<uint32_t *>(scr + (size_t)H * P::kMoves);
 
     for (uint64_t it = 0;; ++it) {
@@ -910,14 +962,19 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         // Owner chores of the round, while the other warps relax: refill the
         // root hole, then drain the insertion buffer down to kBuf - kMoves
         // entries (room for this round's pushes).
-        const auto chores = [&]() {
-            // the buffer's run to drain (its largest entries: the small ones
-            // are popped soon), down to room for this round's pushes
-            uint32_t run = bn > kBuf - P::kMoves ? bn - (kBuf - P::kMoves) : 0u;
+        // The buffer's run to drain (its largest entries: the small ones are
+        // popped soon), down to room for this round's pushes.  An overflow
+        // stops the search at this round's decision, so it is reported before
+        // the owner arrives at the team barrier.
+        uint32_t run = 0;
+        if (owner) {
+            run = bn > kBuf - P::kMoves ? bn - (kBuf - P::kMoves) : 0u;
             if (hs + run > m.hcap) {
-                set_error(&st->err[r3], ST_HEAP_OVERFLOW);  // this round's decision stops the search
+                set_error(&st->err[r3], ST_HEAP_OVERFLOW);
                 run = m.hcap > hs ? m.hcap - hs : 0u;
             }
+        }
+        const auto chores = [&]() {
             // the run's bottom brick is read while the sift-down runs (a
             // fresh bottom brick, at depth 0, needs no read)
             uint32_t pre = 0;
@@ -952,7 +1009,16 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                 bn -= run;
             }
         };
-        if (rfirst > 0 && owner) chores();
+        if (split) {
+            // owner warps: arrive at the team barrier now, refill the heaps,
+            // then wait for the staging (below)
+            if (!relaxer) {
+                team.early_arrive();
+                if (owner) chores();
+            }
+        } else if (rfirst > 0 && owner) {
+            chores();
+        }
         if constexpr (kSort) {
             // every successor's record, at its number in the CTA's list
             if (relaxer) {
@@ -1040,15 +1106,28 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         if (rfirst == 0 && owner) chores();
 
         // publish this CTA's round: its candidate count and claimed slots
-        __syncthreads();
-        if (tid == 0) {
+        const auto publish = [&]() {
             half[(size_t)cta * RR].slot = kSort ? total : *s_cnt;
             if (*s_ins) atomicAdd(&st->ins[r3], (unsigned long long)*s_ins);
             // the time slice is read by one thread of the team, so that all
             // threads take the same decision
             if (cta == 0 && m.deadline_ns) st->quit[r3] = globaltimer_ns() >= m.deadline_ns ? 1u : 0u;
+        };
+        if (!split) {
+            __syncthreads();
+            if (tid == 0) publish();
+            team.sync();
+        } else if (relaxer) {
+            named_sync(2, rthreads);  // every relaxer's counts are in
+            if (tid == rfirst) publish();
+            team.relaxers_sync(T);
+        } else {
+            // Owner warps, chores done: the relaxers arrive at barrier 3 once
+            // they have decided and staged the pushes (or stopped); then the
+            // team barrier has completed too.
+            named_sync(3, T);
+            team.late_wait();
         }
-        team.sync();
 
         // -------------------------------------------------- decision ---
         // Every value read here was written before the barrier above and is
@@ -1070,20 +1149,16 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         if (!err && ins_total > m.max_inserted) err = ST_HASH_FULL;
         const bool pause = ins_total > m.grow_at || (m.deadline_ns && team.rd32(&st->quit[r3]));
         round += 1;
-        if (err) {
+        if (err)
             status = err;
-            break;
-        }
-        if (gbest != kInfCost && P::cost_cmp(gbest, rmin) <= 0) {
+        else if (gbest != kInfCost && P::cost_cmp(gbest, rmin) <= 0)
             status = ST_OK;
-            break;
-        }
-        if (rmin == kInfCost) {
+        else if (rmin == kInfCost)
             status = ST_NO_SOLUTION;
-            break;
-        }
-        if (round >= m.max_rounds) {
+        else if (round >= m.max_rounds)
             status = ST_ITER_LIMIT;
+        if (status != ST_RUNNING) {
+            if (split && relaxer) named_arrive(3, T);  // the owner warps wait there
             break;
         }
 
@@ -1175,7 +1250,10 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
             if (tid == 0 && *s_ins2) atomicAdd(&st->ins[nxt], (unsigned long long)*s_ins2);
         }
         const Cand *const sreg = half + (size_t)src * RR + 1;
-        for (uint32_t q = tid; q < (kSort ? 0u : nshare); q += T) {
+        // (split rounds: the relaxers stage, the owner warps are waiting)
+        const uint32_t q0 = split ? tid - rfirst : tid, qstep = split ? rthreads : T;
+        const uint32_t nstage = kSort || (split && !relaxer) ? 0u : nshare;
+        for (uint32_t q = q0; q < nstage; q += qstep) {
             const Cand c = load_cand(sreg + q);
             E e = prob.make_entry(c.f, c.g, c.slot, c.aux);
             if constexpr (!P::kPrevInKey) {
@@ -1189,7 +1267,10 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
             // popped, and at most one candidate per slot carries its final g)
             stage[q] = e;
         }
-        __syncthreads();
+        if (!split)
+            __syncthreads();
+        else if (relaxer)
+            named_arrive(3, T);
         // The share is dealt round-robin over the CTA's heaps (at most
         // kMoves per heap: the share is at most H * kMoves) into their
         // insertion buffers, which the relax phase left with room for kMoves.
