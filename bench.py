@@ -850,7 +850,7 @@ def main():
     ap.add_argument("--serve-extra-count", type=int, default=2000, help="requests at the lower rates")
     ap.add_argument("--serve-rates", type=lambda s: [float(x) for x in s.split(",")], default=[50.0, 200.0, 1000.0])
     ap.add_argument("--serve-timeout", type=float, default=600.0)
-    ap.add_argument("--plain-budget", type=float, default=420.0,
+    ap.add_argument("--plain-budget", type=float, default=180.0,
                     help="seconds of plain-engine solves over the serving stream")
     ap.add_argument("--check-chunk", type=int, default=2500, help="serving: requests per batched check call")
     ap.add_argument("--no-autotune", action="store_true")

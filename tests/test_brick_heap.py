@@ -143,6 +143,23 @@ class BrickHeap:
             self.sift(self.size, last)
         return out
 
+    def pop_chores(self, run):
+        """A pop followed by the owner's chores (ga_search.cuh): a root taken
+        from the heap is refilled by the run's least entry when there is a run
+        (heapreplace: one sift-down, the last entry stays), else by the last
+        entry; the rest of the run is pushed as one run."""
+        out = self.s[1]
+        self.size -= 1
+        run = sorted(run)
+        if self.size and run:
+            self.size += 1
+            self.sift(self.size, run[0])
+            run = run[1:]
+        elif self.size:
+            self.sift(self.size, self.ld(self.size + 1))
+        self.push_run(run)
+        return out
+
     def sift(self, size, last):
         D, topn = self.D, self.topn()
         now = 1
@@ -273,3 +290,26 @@ def test_a_run_reads_its_bottom_brick_once():
     h.loads = 0
     h.push_run([(10 ** 6 + i,) for i in range(4)])
     assert h.loads == 4
+
+
+@pytest.mark.parametrize("D,L", [(3, 1), (3, 7), (4, 5), (4, 1), (3, 4)])
+def test_pop_with_replace_matches_heapq(D, L):
+    # each round: a pop, then a drained run of 0..4 entries, the least of
+    # which refills the popped root
+    rng = random.Random(D * 11 + L)
+    h = BrickHeap(D, L, 4000)
+    ref = []
+    for _ in range(64):
+        v = (rng.randrange(500), rng.randrange(1 << 20))
+        h.push(v)
+        heapq.heappush(ref, v)
+    for step in range(6000):
+        run = [(rng.randrange(500), rng.randrange(1 << 20)) for _ in range(rng.randrange(0, 5))]
+        if not ref or h.size + len(run) >= h.hcap:
+            break
+        assert h.pop_chores(run) == heapq.heappop(ref)
+        for v in run:
+            heapq.heappush(ref, v)
+        assert h.size == len(ref)
+    while ref:
+        assert h.pop() == heapq.heappop(ref)

@@ -873,7 +873,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         // ------------------------------------------------ phase 1: pop ---
         // The owner takes the root now and refills the hole later in the
         // round (pending_sift), off the path to the successors.
-        bool pending_sift = false;
+        bool pending_sift = false, have_last = false;
         E last;
         if (tid < owner_warps * 32u) {
             E e;
@@ -885,7 +885,13 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                     if (P::less(ibuf[j], ibuf[bi])) bi = j;
                 if (hs > 0 && (bn == 0 || !P::less(ibuf[bi], myheap.s[1]))) {
                     e = myheap.s[1];
-                    last = myheap.ld(hs);
+                    // the heap's last entry refills the root unless the
+                    // buffer has a run to drain (below), whose least entry
+                    // refills it instead
+                    if (bn <= kBuf - P::kMoves) {
+                        last = myheap.ld(hs);
+                        have_last = true;
+                    }
                     hs -= 1;
                     pending_sift = hs > 0;
                 } else {
@@ -975,10 +981,33 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
             }
         }
         const auto chores = [&]() {
-            // the run's bottom brick is read while the sift-down runs (a
+            // the run to the buffer's end, its largest entry last
+            for (uint32_t q = 0; q < run; ++q) {
+                const uint32_t end = bn - 1 - q;
+                uint32_t bx = 0;
+                for (uint32_t j = 1; j <= end; ++j)
+                    if (P::less(ibuf[bx], ibuf[j])) bx = j;
+                const E e = ibuf[bx];
+                ibuf[bx] = ibuf[end];
+                ibuf[end] = e;
+            }
+            // A root taken from the heap is refilled by the run's least entry
+            // (heapreplace): one sift-down serves the pop and one push, and
+            // the heap's last entry stays where it is.  Without a run the
+            // last entry refills it.
+            const bool replace = pending_sift && run > 0;
+            E top = last;
+            if (replace) {
+                top = ibuf[bn - run];
+                hs += 1;
+            } else if (pending_sift && !have_last) {
+                top = myheap.ld(hs + 1);  // (a run cut short by an overflow)
+            }
+            const uint32_t rest = run - (replace ? 1u : 0u);
+            // the rest's bottom brick is read while the sift-down runs (a
             // fresh bottom brick, at depth 0, needs no read)
             uint32_t pre = 0;
-            if (run && hs + 1 > topn) {
+            if (rest && hs + 1 > topn) {
                 uint32_t d;
                 const uint32_t root = myheap.brick_root(hs + 1, &d);
                 if (d > 0) {
@@ -987,7 +1016,7 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                 }
             }
             if (pending_sift) {
-                const uint32_t fin = heap_sift_down<P>(myheap, hs, last);
+                const uint32_t fin = heap_sift_down<P>(myheap, hs, top);
                 // the sift wrote into that brick: its copy is stale
                 if (pre && fin > topn && myheap.brick_root(fin) == pre) {
                     cp_async_wait_all();
@@ -995,19 +1024,8 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                 }
             }
             if (pre) cp_async_wait_all();
-            if (run) {
-                for (uint32_t q = 0; q < run; ++q) {
-                    const uint32_t end = bn - 1 - q;
-                    uint32_t bx = 0;
-                    for (uint32_t j = 1; j <= end; ++j)
-                        if (P::less(ibuf[bx], ibuf[j])) bx = j;
-                    const E e = ibuf[bx];
-                    ibuf[bx] = ibuf[end];
-                    ibuf[end] = e;
-                }
-                heap_push_run<P>(myheap, hs, ibuf + (bn - run), run, pre);
-                bn -= run;
-            }
+            if (rest) heap_push_run<P>(myheap, hs, ibuf + (bn - rest), rest, pre);
+            bn -= run;
         };
         if (split) {
             // owner warps: arrive at the team barrier now, refill the heaps,
