@@ -430,7 +430,7 @@ def section_c4(eng, args):
     # plain engine on a sample of the same mix, one instance at a time
     sample = list(range(0, len(specs), max(1, len(specs) // args.plain_sample)))
     t0 = time.perf_counter()
-    plain_ok = 0
+    plain_ok = plain_exp = 0
     for i in sample:
         s, inst = specs[i], insts[i]
         if isinstance(s, WL.PuzzleSpec):
@@ -439,7 +439,9 @@ def section_c4(eng, args):
         else:
             r = eng.grid_solve(inst.words, s.H, s.W, s.start, s.goal)
             plain_ok += int(r.ok and (r.straight, r.diagonal) == (res[i]["straight"], res[i]["diagonal"]))
-    plain = len(sample) / (time.perf_counter() - t0)
+        plain_exp += r.expanded
+    plain_s = time.perf_counter() - t0
+    plain = len(sample) / plain_s
     agree = None
     rows = golden("mixed_c4.json")
     if rows:
@@ -457,7 +459,13 @@ def section_c4(eng, args):
            "threads_per_instance": st["threads_per_instance"], "heap_capacity": st["heap_capacity"],
            "load_factor": st["load_factor"], "autotune": tune, "all_ok": all(r["status"] == 0 for r in res),
            "plain_sample": f"{len(sample)} instances (every {len(specs) // len(sample)}th)",
-           "plain_agrees": f"{plain_ok}/{len(sample)}", "optimal_agreement": agree}
+           "plain_agrees": f"{plain_ok}/{len(sample)}", "optimal_agreement": agree,
+           # the ratio = (aggregate expansion rate ratio) x (expansions per solve, plain / batched)
+           "plain_expanded_per_s": round(plain_exp / plain_s, 1),
+           "expansions_per_solve": {"batched": round(st["expanded"] / len(insts)),
+                                    "batched_on_plain_sample": round(sum(res[i]["expanded"] for i in sample)
+                                                                     / len(sample)),
+                                    "plain_on_plain_sample": round(plain_exp / len(sample))}}
     if args.cpu_sections:
         order = seeded_order(len(specs), 0xC4)
         out["cpu_baseline"] = cpu_baseline_stream(eng, [specs[i] for i in order], os.cpu_count() or 1,
@@ -516,7 +524,9 @@ def serve_run(eng, stream, rate: float, args) -> tuple[dict, dict]:
            "p99_ms": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3) if lat else None,
            "quanta": st["quanta"], "peak_resident": st["peak_resident"],
            "peak_budget_gb": round(st["peak_budget_gb"], 2),
-           "migrations": sum(r.get("migrations", 0) for r in got.values())}
+           "migrations": sum(r.get("migrations", 0) for r in got.values()),
+           "expanded_per_s": round(sum(r["expanded"] for r in got.values() if r["status"] == 0)
+                                   / max(done_t, 1e-9), 1)}
     return row, got
 
 
@@ -560,7 +570,7 @@ def section_c5(eng, args):
                               f"({time.perf_counter() - t0:.0f} s)"
     # the plain engine, one request at a time, in stream order, under a time guard
     t0 = time.perf_counter()
-    n = agree = 0
+    n = agree = exp = 0
     for i, (_, spec) in enumerate(stream):
         if time.perf_counter() - t0 > args.plain_budget:
             break
@@ -571,10 +581,16 @@ def section_c5(eng, args):
             r = eng.grid_solve(spec.words(), spec.H, spec.W, spec.start, spec.goal)
             ref = {"straight": r.straight, "diagonal": r.diagonal}
         n += 1
+        exp += r.expanded
         agree += int(r.ok and same_result(spec, served.get(i), ref))
     plain_s = time.perf_counter() - t0
     plain = n / plain_s
     out["plain_solves_per_s"] = round(plain, 2)
+    # the ratio = (aggregate expansion rate ratio) x (expansions per solve, plain / served)
+    out["plain_expanded_per_s"] = round(exp / plain_s, 1)
+    out["expansions_per_solve"] = {
+        "plain": round(exp / max(n, 1)),
+        "served_same_requests": round(sum(served[i]["expanded"] for i in range(n) if i in served) / max(n, 1))}
     out["plain_compared"] = f"{agree}/{n} of {len(stream)} served results equal the plain engine's " \
                             f"(stream order, {plain_s:.0f} s time guard {args.plain_budget:.0f} s)"
     for row in out["rates"]:

@@ -99,3 +99,27 @@ def test_wide_searches_move_to_cluster_slots(seng):
             assert r["status"] == L.OK and p.ok
             assert (r["straight"], r["diagonal"]) == (p.straight, p.diagonal)
             assert float_equal(r["cost"], p.cost)
+
+
+def test_serving_after_a_batch_and_a_failed_allocation():
+    # A batch leaves its team regions cached on the engine; the serving loop
+    # takes its budget after them, and a serving budget that cannot be had
+    # fails alone: the engine keeps working.
+    from uastar_gb300 import EngineError
+    with Engine(0) as eng:
+        eng.pdb_build(4)
+        insts = [s.instance() for s in WL.mixed_1024()[::8]]
+        res, _ = eng.batch_solve(insts, load_factor=0.35)
+        assert all(r["status"] == L.OK for r in res)
+        with pytest.raises(EngineError):
+            eng.serve_start(hbm_budget_gb=1e6)
+        row = WL.puzzle15_x100(count=1)[0]
+        assert eng.puzzle_solve(4, row.tiles()).ok
+        eng.serve_start(hbm_budget_gb=120.0)
+        reqs = [s.instance() for _, s in WL.serve_stream(16, 1000.0, max_side=512, walks=(20, 60))]
+        ids = [eng.serve_submit(inst) for inst in reqs]
+        got = drain(eng, len(ids))
+        eng.serve_stop(30.0)
+        assert len(got) == len(ids) and all(r["status"] == L.OK for r in got.values())
+        res2, _ = eng.batch_solve(insts[:32])  # and a batch after serving
+        assert all(r["status"] == L.OK for r in res2)

@@ -94,13 +94,13 @@ struct BatchArgs {
 // returns their number, or cap + 1 if the chain is longer than cap.  One
 // thread: a pointer chase.
 __device__ unsigned long long walk_chain(const Slot *part, uint32_t goal_slot, unsigned long long *out,
-                                         uint64_t cap, bool prev_in_key) {
+                                         uint64_t cap, int link) {
     uint32_t s = goal_slot;
     uint64_t n = 0;
     while (s != kNone && n < cap) {
         uint64_t key;
         uint32_t prev;
-        slot_key_prev(part + s, prev_in_key, key, prev);
+        slot_key_prev(part + s, link, key, prev);
         out[n++] = key;
         s = prev;
     }
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
             // team's next instance)
             if (o.status == ST_OK)
                 o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap,
-                                        d.kind == UASTAR_KIND_GRID && GridProblem::kPrevInKey);
+                                        d.kind == UASTAR_KIND_GRID ? GridProblem::kLink : PuzzleProblem<4>::kLink);
             a.outs[i] = o;
             if (a.serving) a.states[i] = st;
         }
@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(512, 1) k_batch_cluster(BatchArgs a) {
             if (o.status == ST_RUNNING && pend) o.status = pend;
             if (o.status == ST_OK)
                 o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap,
-                                        d.kind == UASTAR_KIND_GRID && GridProblem::kPrevInKey);
+                                        d.kind == UASTAR_KIND_GRID ? GridProblem::kLink : PuzzleProblem<4>::kLink);
             a.outs[i] = o;
         }
         team.sync();
@@ -307,7 +307,7 @@ __global__ void k_batch_walk(const InstDesc *descs, const InstOut *outs, const u
     if (t >= nwhich) return;
     const uint32_t i = which[t];
     lens[t] = walk_chain(tab + descs[i].tab_off, outs[i].goal_slot, keys + key_off[t], key_cap[t],
-                         descs[i].kind == UASTAR_KIND_GRID && GridProblem::kPrevInKey);
+                         descs[i].kind == UASTAR_KIND_GRID ? GridProblem::kLink : PuzzleProblem<4>::kLink);
 }
 
 // Move a parked single-CTA search's heaps (hs heaps) onto a cluster slot's
@@ -797,6 +797,13 @@ int32_t run_wave(uastar_engine *eng, const uastar_instance *insts, const std::ve
 }
 
 }  // namespace
+
+namespace uastar {
+void release_batch_buffers(uastar_engine *eng) {
+    for (DevBuf *b : {&eng->b_tab, &eng->b_heaps, &eng->b_bitmaps, &eng->b_cand, &eng->b_hsize, &eng->b_walk})
+        b->release();
+}
+}  // namespace uastar
 
 extern "C" {
 
@@ -1432,10 +1439,10 @@ static void serve_grow(ServeState *S, ServeTier &t, int q) {
     fill_ff_async(eng, dst, new_n * sizeof(Slot), t.stream);
     if (d.kind == UASTAR_KIND_GRID) {
         k_grow_move<false, GridProblem::kPrevInKey><<<blocks, 256, 0, t.stream>>>(src, old_n, dst, new_n - 1, map);
-        k_grow_links<false, GridProblem::kPrevInKey><<<blocks, 256, 0, t.stream>>>(src, old_n, dst, map);
+        k_grow_links<false, GridProblem::kLink><<<blocks, 256, 0, t.stream>>>(src, old_n, dst, map);
     } else {
         k_grow_move<false, false><<<blocks, 256, 0, t.stream>>>(src, old_n, dst, new_n - 1, map);
-        k_grow_links<false, false><<<blocks, 256, 0, t.stream>>>(src, old_n, dst, map);
+        k_grow_links<false, PuzzleProblem<4>::kLink><<<blocks, 256, 0, t.stream>>>(src, old_n, dst, map);
     }
     if (d.kind == UASTAR_KIND_GRID)
         k_grow_heaps<GridProblem><<<blocks, 256, 0, t.stream>>>(
@@ -1804,6 +1811,9 @@ int32_t uastar_serve_start(uastar_engine *eng, const uastar_serve_config *cfg) {
         return UASTAR_BAD_INPUT;
     }
     cudaSetDevice(eng->device);
+    // the serving arenas take the budget: the batched engine's cached
+    // buffers go back first (a later batch call allocates them again)
+    release_batch_buffers(eng);
     auto *S = new ServeState();
     S->eng = eng;
     if (cfg) S->cfg = *cfg;

@@ -110,14 +110,14 @@ __global__ void __launch_bounds__(512, 1) k_round_floor(TeamState *st, uint64_t 
 // Walk the prev chain from the goal slot (one thread: a pointer chase).
 // Writes keys goal -> start; *len = count, or cap + 1 when truncated.
 __global__ void k_walk(const Slot *tab, uint32_t goal_slot, unsigned long long *keys,
-                       uint64_t cap, unsigned long long *len, bool prev_in_key) {
+                       uint64_t cap, unsigned long long *len, int link) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     uint32_t s = goal_slot;
     uint64_t n = 0;
     while (s != kNone && n < cap) {
         uint64_t key;
         uint32_t prev;
-        slot_key_prev(tab + s, prev_in_key, key, prev);
+        slot_key_prev(tab + s, link, key, prev);
         keys[n++] = key;
         s = prev;
     }
@@ -230,7 +230,12 @@ bool grow_table(uastar_engine *eng, SearchMem<typename P::Entry> &m, uint32_t k,
     const size_t need = (new_n * sizeof(Slot) > eng->tab_next.bytes ? new_n * sizeof(Slot) : 0) +
                         (old_n * 4 > eng->grow_map.bytes ? old_n * 4 : 0);
     // at most 2^31 slots: every slot index stays below the no-parent mark kNone
-    if (new_n > (1ull << 31) || need + (256ull << 20) > free_b) return false;
+    if (new_n > (1ull << 31)) return false;
+    if (need + (256ull << 20) > free_b) {  // the batched engine's cached buffers give way
+        release_batch_buffers(eng);
+        cudaMemGetInfo(&free_b, &total_b);
+        if (need + (256ull << 20) > free_b) return false;
+    }
     if (eng->tab_next.ensure(new_n * sizeof(Slot)) != cudaSuccess) return false;
     if (eng->grow_map.ensure(old_n * 4) != cudaSuccess) return false;
     if (fill_ff(eng, eng->tab_next.p, new_n * sizeof(Slot)) != UASTAR_OK) return false;
@@ -238,7 +243,7 @@ bool grow_table(uastar_engine *eng, SearchMem<typename P::Entry> &m, uint32_t k,
     Slot *src = m.tab, *dst = eng->tab_next.as<Slot>();
     uint32_t *map = eng->grow_map.as<uint32_t>();
     k_grow_move<P::kWide, P::kPrevInKey><<<blocks, 256, 0, eng->stream>>>(src, old_n, dst, new_n - 1, map);
-    k_grow_links<P::kWide, P::kPrevInKey><<<blocks, 256, 0, eng->stream>>>(src, old_n, dst, map);
+    k_grow_links<P::kWide, P::kLink><<<blocks, 256, 0, eng->stream>>>(src, old_n, dst, map);
     k_grow_heaps<P><<<blocks, 256, 0, eng->stream>>>(m.heaps, m.stride, m.L, m.heap_size, k, map, st);
     eng->launches += 3;
     if (cudaGetLastError() != cudaSuccess) return false;
@@ -324,8 +329,17 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
         const size_t tab_b = slots * sizeof(Slot);
         const size_t heap_b = (size_t)k * hg.stride * sizeof(E);
         const size_t cand_b = cand_records<P>(nblocks, H) * sizeof(Cand);
-        if ((e = eng->tab.ensure(tab_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc table");
-        if ((e = eng->heaps.ensure(heap_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc heaps");
+        // the batched engine's cached buffers give way to a table that does not fit
+        if ((e = eng->tab.ensure(tab_b)) != cudaSuccess) {
+            release_batch_buffers(eng);
+            e = eng->tab.ensure(tab_b);
+        }
+        if (e != cudaSuccess) return fail_cuda(eng, e, "alloc table");
+        if ((e = eng->heaps.ensure(heap_b)) != cudaSuccess) {
+            release_batch_buffers(eng);
+            e = eng->heaps.ensure(heap_b);
+        }
+        if (e != cudaSuccess) return fail_cuda(eng, e, "alloc heaps");
         if ((e = eng->heap_size.ensure((size_t)k * 4)) != cudaSuccess) return fail_cuda(eng, e, "alloc heap sizes");
         if ((e = eng->cand.ensure(cand_b)) != cudaSuccess) return fail_cuda(eng, e, "alloc candidates");
         if ((e = eng->team.ensure(sizeof(TeamState))) != cudaSuccess) return fail_cuda(eng, e, "alloc state");
@@ -423,14 +437,13 @@ int32_t run_plain(uastar_engine *eng, const P &prob, int log2_auto, uint32_t str
     return UASTAR_OK;
 }
 
-int32_t walk_keys(uastar_engine *eng, uint32_t goal_slot, uint64_t cap, std::vector<uint64_t> *keys,
-                  bool prev_in_key) {
+int32_t walk_keys(uastar_engine *eng, uint32_t goal_slot, uint64_t cap, std::vector<uint64_t> *keys, int link) {
     cudaError_t e;
     const size_t need = (size_t)cap * 8 + 64;
     if ((e = eng->walk.ensure(need)) != cudaSuccess) return fail_cuda(eng, e, "alloc walk");
     unsigned long long *d_keys = eng->walk.as<unsigned long long>();
     unsigned long long *d_len = d_keys + cap;
-    k_walk<<<1, 32, 0, eng->stream>>>(eng->tab.as<Slot>(), goal_slot, d_keys, cap, d_len, prev_in_key);
+    k_walk<<<1, 32, 0, eng->stream>>>(eng->tab.as<Slot>(), goal_slot, d_keys, cap, d_len, link);
     eng->launches++;
     if ((e = cudaGetLastError()) != cudaSuccess) return fail_cuda(eng, e, "walk launch");
     unsigned long long len = 0;
@@ -564,7 +577,7 @@ int32_t grid_solve_impl(uastar_engine *eng, const uint64_t *host_words, int32_t 
         // Path: walk prev pointers on the device, re-validate on the host.
         std::vector<uint64_t> keys;
         const uint64_t cap = std::min<uint64_t>(cells + 1, 1ull << 26);
-        rc = walk_keys(eng, st.goal_slot, cap, &keys, GridProblem::kPrevInKey);
+        rc = walk_keys(eng, st.goal_slot, cap, &keys, GridProblem::kLink);
         if (rc) return out->status = rc;
         eng->path.assign(keys.size(), 0);
         for (size_t i = 0; i < keys.size(); ++i) eng->path[i] = (int32_t)keys[i];
@@ -644,7 +657,7 @@ int32_t walk_boards(uastar_engine *eng, uint32_t slot, std::vector<std::vector<u
         }
     } else {
         std::vector<uint64_t> keys;
-        if (int32_t rc = walk_keys(eng, slot, 4096, &keys, false)) return rc;
+        if (int32_t rc = walk_keys(eng, slot, 4096, &keys, PuzzleProblem<4>::kLink)) return rc;
         for (uint64_t k : keys) {
             std::vector<uint8_t> b(N * N);
             for (int c = 0; c < N * N; ++c) b[c] = (uint8_t)((k >> (4 * c)) & 15);
@@ -1170,7 +1183,7 @@ int32_t uastar_puzzle_solve(uastar_engine *eng, int32_t n, const uint8_t *tiles,
             }
         } else {
             std::vector<uint64_t> keys;
-            rc = walk_keys(eng, st.goal_slot, 4096, &keys, false);
+            rc = walk_keys(eng, st.goal_slot, 4096, &keys, PuzzleProblem<4>::kLink);
             if (rc) return out->status = rc;
             for (uint64_t k : keys) {
                 int b = -1;

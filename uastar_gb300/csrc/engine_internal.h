@@ -30,7 +30,10 @@ struct DevBuf {
         p = nullptr;
         bytes = 0;
         cudaError_t e = cudaMalloc(&p, need);
-        if (e == cudaSuccess) bytes = need;
+        if (e == cudaSuccess)
+            bytes = need;
+        else
+            (void)cudaGetLastError();  // an allocation failure is reported here, not by the next launch check
         return e;
     }
     void release() {
@@ -126,4 +129,8 @@ int32_t fail_cuda(uastar_engine *eng, cudaError_t e, const char *what);
 int32_t fill_ff_async(uastar_engine *eng, void *p, size_t bytes, cudaStream_t stream);
 // pdb.cu
 int32_t pdb_build_device(uastar_engine *eng, int n, double *ms);
+// batch.cu: the batched engine keeps its team regions, heaps and bitmaps for
+// the next batch; a caller that needs the memory (the serving loop, a plain
+// solve that cannot get its table) gives them back.
+void release_batch_buffers(uastar_engine *eng);
 }  // namespace uastar

@@ -54,10 +54,21 @@ struct __align__(32) WideSlot {
 };
 static_assert(sizeof(WideSlot) == 32, "wide slot must be one sector");
 
+// Where a slot keeps its parent link: its own field, written after the
+// round's barrier by the candidate that won the slot; the key word (grids:
+// cell | prev << 32); or the g word (narrow puzzle keys: g << 40 | (last
+// move + 1) << 32 | prev).  In the key or the g word the link is set by the
+// same 16-byte CAS that sets g, so the push phase checks no winner.
+enum SlotLink : int { LINK_FIELD = 0, LINK_IN_KEY = 1, LINK_IN_G = 2 };
+
 struct NarrowSlots {
     using Key = uint64_t;
     static constexpr bool kWide = false;
     static constexpr bool kPrevInKey = false;  // see GridProblem
+    static constexpr int kLink = LINK_FIELD;
+    // the g word that the relax CAS installs, and its cost
+    __device__ static uint64_t g_word(uint64_t g, uint32_t, int) { return g; }
+    __device__ static uint64_t word_g(uint64_t w) { return w; }
     __device__ static uint64_t slot_g(const Slot *s) { return __ldcg(&s->g); }
     __device__ static uint32_t slot_prev(const Slot *s) { return __ldcg(&s->prev); }
     __device__ static void set_link(Slot *s, uint32_t prev, uint32_t aux) {
@@ -69,6 +80,7 @@ struct WideSlots {
     using Key = Key128;
     static constexpr bool kWide = true;
     static constexpr bool kPrevInKey = false;
+    static constexpr int kLink = LINK_FIELD;
     __device__ static const WideSlot *w(const Slot *s) { return reinterpret_cast<const WideSlot *>(s); }
     __device__ static WideSlot *w(Slot *s) { return reinterpret_cast<WideSlot *>(s); }
     __device__ static uint64_t slot_g(const Slot *s) { return __ldcg(&w(s)->g); }
@@ -79,16 +91,16 @@ struct WideSlots {
     }
 };
 
-// Key and parent link of a narrow slot; with the link in the key word
-// (grids) the word is cell | prev << 32.  For the path walkers.
-__device__ __forceinline__ void slot_key_prev(const Slot *s, bool prev_in_key, uint64_t &key, uint32_t &prev) {
+// Key and parent link of a narrow slot (`link`: a SlotLink).  For the path
+// walkers.
+__device__ __forceinline__ void slot_key_prev(const Slot *s, int link, uint64_t &key, uint32_t &prev) {
     const uint64_t w = __ldcg(&s->key);
-    if (prev_in_key) {
+    if (link == LINK_IN_KEY) {
         key = w & 0xffffffffull;
         prev = (uint32_t)(w >> 32);
     } else {
         key = w;
-        prev = __ldcg(&s->prev);
+        prev = link == LINK_IN_G ? (uint32_t)__ldcg(&s->g) : __ldcg(&s->prev);
     }
 }
 

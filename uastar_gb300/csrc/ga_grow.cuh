@@ -49,14 +49,19 @@ __global__ void k_grow_move(const Slot *src, uint64_t n, Slot *dst, uint64_t mas
     }
 }
 
-template <bool Wide, bool PrevInKey>
+// Link: where the slots keep their parent link (SlotLink).
+template <bool Wide, int Link>
 __global__ void k_grow_links(const Slot *src, uint64_t n, Slot *dst, const uint32_t *map) {
     for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t w = __ldcg(&src[s].key);
         if (w == kEmptyKey) continue;
-        if constexpr (PrevInKey) {
+        if constexpr (Link == LINK_IN_KEY) {
             const uint32_t p = (uint32_t)(w >> 32);
             dst[map[s]].key = (w & 0xffffffffull) | (uint64_t)(p == kNone ? kNone : map[p]) << 32;
+        } else if constexpr (Link == LINK_IN_G) {
+            const uint64_t gw = __ldcg(&src[s].g);
+            const uint32_t p = (uint32_t)gw;
+            dst[map[s]].g = (gw & ~0xffffffffull) | (p == kNone ? kNone : map[p]);
         } else if constexpr (Wide) {
             const uint32_t p = __ldcg(&WideSlots::w(src + s)->prev);
             WideSlots::w(dst + map[s])->prev = p == kNone ? kNone : map[p];

@@ -47,6 +47,7 @@ struct GridProblem : NarrowSlots {
     // Slot key word = cell | prev << 32 (cells are < 2^32 - 1): the relax CAS
     // sets g and the parent link together, so no push-phase winner check.
     static constexpr bool kPrevInKey = true;
+    static constexpr int kLink = LINK_IN_KEY;
     __device__ static uint32_t slot_prev(const Slot *s) { return (uint32_t)(__ldcg(&s->key) >> 32); }
     __device__ static void set_link(Slot *, uint32_t, uint32_t) {}  // the link lives in the key word
 
@@ -272,6 +273,19 @@ template <int N> struct PuzzleProblem : NarrowSlots {
     using Entry = PuzzleEntry;
     static constexpr int kMoves = 4;
     static constexpr int NN = N * N;
+    // The slot's g word is g << 40 | (last move + 1) << 32 | prev: the relax
+    // CAS sets the cost and the path link together, so the push phase checks
+    // no winner (a candidate that lost is a stale entry, dropped at its pop).
+    // The aux field keeps the pattern parts, which depend on the board alone:
+    // the relaxer that claims the slot writes them.
+    static constexpr int kLink = LINK_IN_G;
+    __device__ static uint64_t g_word(uint64_t g, uint32_t prev, int mv) {
+        return g << 40 | (uint64_t)(uint32_t)(mv + 1) << 32 | prev;
+    }
+    __device__ static uint64_t word_g(uint64_t w) { return w >> 40; }
+    __device__ static uint64_t slot_g(const Slot *s) { return __ldcg(&s->g) >> 40; }
+    __device__ static uint32_t slot_prev(const Slot *s) { return (uint32_t)__ldcg(&s->g); }
+    __device__ static void set_link(Slot *s, uint32_t, uint32_t aux) { s->aux = aux & 0xffffu; }
 
     const uint8_t *pdb;   // concatenated tables
     uint64_t start;       // packed board: cell i at bits 4i
@@ -409,8 +423,8 @@ template <int N> struct PuzzleProblem : NarrowSlots {
                                                      uint32_t &aux) {
         const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(s));
         key = v.x;
-        g = v.y;
-        aux = __ldcg(&s->aux);
+        g = v.y >> 40;
+        aux = (__ldcg(&s->aux) & 0xffffu) | ((uint32_t)(v.y >> 32) & 0xffu) << kLastMoveShift;
     }
 };
 

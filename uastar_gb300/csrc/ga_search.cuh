@@ -543,7 +543,9 @@ enum : int { RELAX_NONE = 0, RELAX_IMPROVED = 1, RELAX_CLAIMED = 2, RELAX_INSERT
 // Where the problem keeps the parent link in the key word (P::kPrevInKey:
 // grid cells are 32 bits), the word is cell | prev << 32 and the CAS sets g
 // and prev together, so the slot's link always belongs to its g: the push
-// phase then needs no winner check.  Keys compare on the cell half.
+// phase then needs no winner check.  Keys compare on the cell half.  Where it
+// keeps the link in the g word (P::kLink == LINK_IN_G), the CAS installs
+// P::g_word(g, prev, move) and costs compare on P::word_g of it.
 template <class P> __device__ __forceinline__ bool key_match(uint64_t word, uint64_t key) {
     if constexpr (P::kPrevInKey)
         return (word & 0xffffffffull) == key && word != kEmptyKey;
@@ -553,12 +555,12 @@ template <class P> __device__ __forceinline__ bool key_match(uint64_t word, uint
 
 template <class P>
 __device__ __forceinline__ int relax_at(Slot *tab, uint64_t h, KeyG cur, uint64_t word, uint64_t g,
-                                        uint32_t *slot_out) {
-    // the slot holds the key: lower g (and, with the link in the key word,
-    // set the link with it)
+                                        uint64_t gw, uint32_t *slot_out) {
+    // the slot holds the key: lower g (and, with the link in the key or g
+    // word, set the link with it)
     *slot_out = (uint32_t)h;
-    while (P::cost_cmp(g, cur.g) < 0) {
-        const KeyG old = cas128(tab + h, cur, KeyG{P::kPrevInKey ? word : cur.key, g});
+    while (P::cost_cmp(g, P::word_g(cur.g)) < 0) {
+        const KeyG old = cas128(tab + h, cur, KeyG{P::kPrevInKey ? word : cur.key, gw});
         if (old.key == cur.key && old.g == cur.g) return RELAX_IMPROVED;
         cur = old;
     }
@@ -567,19 +569,20 @@ __device__ __forceinline__ int relax_at(Slot *tab, uint64_t h, KeyG cur, uint64_
 
 template <class P>
 __device__ __forceinline__ int relax(Slot *tab, uint64_t mask, uint32_t max_probe, uint64_t key, uint64_t g,
-                                     uint32_t prev, uint32_t *slot_out) {
+                                     uint32_t prev, uint32_t *slot_out, int mv = -1) {
     // Linear probing.  The home slot is tried with one 16-byte CAS; past it
     // the probe reads the rest of the home slot's 128-byte line (4 slots) and
     // then whole lines, one dependent load per line.
     const uint64_t word = P::kPrevInKey ? (key | (uint64_t)prev << 32) : key;
+    const uint64_t gw = P::g_word(g, prev, mv);
     uint64_t h = mix64(key) & mask;
     const KeyG empty{kEmptyKey, kInfCost};
-    KeyG cur = cas128(tab + h, empty, KeyG{word, g});
+    KeyG cur = cas128(tab + h, empty, KeyG{word, gw});
     if (cur.key == kEmptyKey) {
         *slot_out = (uint32_t)h;
         return RELAX_INSERTED;
     }
-    if (key_match<P>(cur.key, key)) return relax_at<P>(tab, h, cur, word, g, slot_out);
+    if (key_match<P>(cur.key, key)) return relax_at<P>(tab, h, cur, word, g, gw, slot_out);
     uint32_t probed = 1;
     h = (h + 1) & mask;
     while (probed < max_probe) {
@@ -591,14 +594,14 @@ __device__ __forceinline__ int relax(Slot *tab, uint64_t mask, uint32_t max_prob
             if (q < n) v[q] = __ldcg(reinterpret_cast<const ulonglong2 *>(tab + h + q));
         for (uint32_t q = 0; q < n; ++q) {
             const uint64_t hq = h + q;
-            if (key_match<P>(v[q].x, key)) return relax_at<P>(tab, hq, KeyG{v[q].x, v[q].y}, word, g, slot_out);
+            if (key_match<P>(v[q].x, key)) return relax_at<P>(tab, hq, KeyG{v[q].x, v[q].y}, word, g, gw, slot_out);
             if (v[q].x == kEmptyKey) {
-                cur = cas128(tab + hq, empty, KeyG{word, g});
+                cur = cas128(tab + hq, empty, KeyG{word, gw});
                 if (cur.key == kEmptyKey) {
                     *slot_out = (uint32_t)hq;
                     return RELAX_INSERTED;
                 }
-                if (key_match<P>(cur.key, key)) return relax_at<P>(tab, hq, cur, word, g, slot_out);
+                if (key_match<P>(cur.key, key)) return relax_at<P>(tab, hq, cur, word, g, gw, slot_out);
                 // another key took it: keep probing
             }
         }
@@ -637,11 +640,11 @@ __device__ __forceinline__ int relax_wide(Slot *tab, uint64_t mask, uint32_t max
 
 template <class P>
 __device__ __forceinline__ int relax_key(Slot *tab, uint64_t mask, uint32_t max_probe, const typename P::Key &key,
-                                         uint64_t g, uint32_t prev, uint32_t *slot_out) {
+                                         uint64_t g, uint32_t prev, uint32_t *slot_out, int mv = -1) {
     if constexpr (P::kWide)
         return relax_wide<P>(tab, mask, max_probe, key, g, slot_out);
     else
-        return relax<P>(tab, mask, max_probe, key, g, prev, slot_out);
+        return relax<P>(tab, mask, max_probe, key, g, prev, slot_out, mv);
 }
 
 __device__ __forceinline__ Cand load_cand(const Cand *p) {
@@ -1091,13 +1094,17 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
                     prob.succ_begin(pi.key, pi.g, pi.aux, move, sc);
                     ng = sc.g;
                     ++nS;
-                    const int r = relax_key<P>(m.tab, m.mask, m.max_probe, sc.key, sc.g, oslot, &nslot);
+                    const int r = relax_key<P>(m.tab, m.mask, m.max_probe, sc.key, sc.g, oslot, &nslot, move);
                     prob.succ_end(sc, pi.aux, move, naux, nf);
                     if (r == RELAX_FULL) {
                         set_error(&st->err[r3], ST_HASH_FULL);
                     } else {
                         inserted = (r & RELAX_CLAIMED) != 0;
                         improved = (r & RELAX_IMPROVED) != 0;
+                        // (link in the g word: the claimer stores the node's
+                        // pattern parts, the same for every writer of the key)
+                        if constexpr (P::kLink == LINK_IN_G)
+                            if (inserted) P::set_link(m.tab + nslot, oslot, naux);
                     }
                 }
                 const uint32_t ib = __ballot_sync(kFull, inserted);
@@ -1274,15 +1281,16 @@ __device__ uint32_t ga_search(const P &prob, Team &team, const SearchMem<typenam
         for (uint32_t q = q0; q < nstage; q += qstep) {
             const Cand c = load_cand(sreg + q);
             E e = prob.make_entry(c.f, c.g, c.slot, c.aux);
-            if constexpr (!P::kPrevInKey) {
+            if constexpr (P::kLink == LINK_FIELD) {
                 if (P::slot_g(m.tab + c.slot) == c.g)
                     P::set_link(m.tab + c.slot, c.parent, c.aux);
                 else
                     e.slot = kNone;  // lost to a better writer
             }
-            // (link in the key word: every candidate is pushed; one that lost
-            // to a better writer of the round is a stale entry, dropped when
-            // popped, and at most one candidate per slot carries its final g)
+            // (link in the key or g word: every candidate is pushed; one that
+            // lost to a better writer of the round is a stale entry, dropped
+            // when popped, and at most one candidate per slot carries its
+            // final g)
             stage[q] = e;
         }
         if (!split)

@@ -115,7 +115,7 @@ __global__ void k_noalloc_finish(const unsigned char *scratch, int32_t *path, in
             while (s != kNone && n < cap) {
                 uint64_t key;
                 uint32_t prev;
-                slot_key_prev(tab + s, GridProblem::kPrevInKey, key, prev);
+                slot_key_prev(tab + s, GridProblem::kLink, key, prev);
                 path[n++] = (int32_t)key;
                 s = prev;
             }
