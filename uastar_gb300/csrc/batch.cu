@@ -1105,6 +1105,9 @@ struct ServeTier {
     cudaEvent_t e0 = nullptr, e1 = nullptr, done = nullptr;
     bool inflight = false;
     std::vector<char> launched;  // slots that are part of the quantum in flight
+    // dedup ranges left by growths queued on this tier's stream: released
+    // when its next quantum has finished, which the growth kernels precede
+    std::vector<std::pair<uint64_t, uint64_t>> release_after;
     int resident() const {
         int n = 0;
         for (auto &sl : slots) n += sl.busy;
@@ -1424,6 +1427,11 @@ static void serve_grow(ServeState *S, ServeTier &t, int q) {
         d.grow_at = 0;
         return;
     }
+    // a larger map replaces the one that growths queued earlier may still read
+    if (old_n * 4 > t.d_map.bytes && cudaStreamSynchronize(t.stream) != cudaSuccess) {
+        S->loop_error = UASTAR_CUDA_ERROR;
+        return;
+    }
     if (t.d_map.ensure(old_n * 4) != cudaSuccess) {
         S->tab_alloc.release(noff, new_n);
         d.grow_at = 0;
@@ -1453,12 +1461,14 @@ static void serve_grow(ServeState *S, ServeTier &t, int q) {
             reinterpret_cast<PuzzleEntry *>(S->heaps.as<uint8_t>() + d.heap_off), d.heap_stride, t.geo.L_puzzle,
             hsize, k, map, st);
     eng->launches += 4;
-    // the old range may be handed out (and cleared on another stream) once released
-    if (cudaStreamSynchronize(t.stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+    if (cudaGetLastError() != cudaSuccess) {
         S->loop_error = UASTAR_CUDA_ERROR;
         return;
     }
-    S->tab_alloc.release(sl.tab_off, sl.tab_n);
+    // The old range may be handed out (and cleared on another stream) only
+    // once the growth kernels have read it: it is released when this tier's
+    // next quantum, queued behind them, has finished (no host wait here).
+    t.release_after.emplace_back(sl.tab_off, sl.tab_n);
     sl.tab_off = noff;
     sl.tab_n = new_n;
     d.tab_off = noff;
@@ -1544,6 +1554,8 @@ static bool serve_migrate(ServeState *S, int q) {
 // which a cluster would not shorten.
 static void serve_retire(ServeState *S, ServeTier &t, std::deque<ServeReq> &to_large, bool spare) {
     ServeTier &large = S->tier[1];
+    for (const auto &r : t.release_after) S->tab_alloc.release(r.first, r.second);
+    t.release_after.clear();
     float ms = 0;
     cudaEventElapsedTime(&ms, t.e0, t.e1);
     S->stats.quanta += 1;
