@@ -87,8 +87,16 @@ struct BatchArgs {
     int serving;           // 1: CTA b serves slot b; 0: work queue
     uint64_t region_slots; // batch: dedup region of each team (reused by the instances it takes)
     uint64_t quantum_ns;   // serving: time slice of the launch, from each team's start (0: rounds only)
+    uint64_t walk_inline;  // serving: paths of more cells are walked after the quantum (0: all inline)
     unsigned long long *keys;  // batch: path keys of solved instances
 };
+
+// Cells (states) on the path of a solved instance, from its goal cost: a
+// grid's straight + diagonal steps, a puzzle's moves, plus the start.
+__host__ __device__ inline uint64_t path_cells(uint32_t kind, unsigned long long goal_best) {
+    return kind == UASTAR_KIND_GRID ? (goal_best >> 32) + (goal_best & 0xffffffffull) + 1 : goal_best + 1;
+}
+constexpr unsigned long long kWalkDeferred = ~0ull;  // InstOut::path_len: walk after the quantum
 
 // Writes the keys of the prev chain from `goal_slot` (goal -> start) and
 // returns their number, or cap + 1 if the chain is longer than cap.  One
@@ -217,15 +225,27 @@ __global__ void __launch_bounds__(512, 1) k_batch(BatchArgs a) {
             // an error of a parked search is reported by its next decision: report it now
             if (o.status == ST_RUNNING && st.error) o.status = st.error;
             // the path is read out now (a batch region is reused by the
-            // team's next instance)
-            if (o.status == ST_OK)
-                o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap,
-                                        d.kind == UASTAR_KIND_GRID ? GridProblem::kLink : PuzzleProblem<4>::kLink);
+            // team's next instance); a serving request's long path is walked
+            // after the quantum instead, so that one thread's pointer chase
+            // does not hold the whole launch
+            if (o.status == ST_OK) {
+                if (a.walk_inline && path_cells(d.kind, o.goal_best) > a.walk_inline)
+                    o.path_len = kWalkDeferred;
+                else
+                    o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap,
+                                            d.kind == UASTAR_KIND_GRID ? GridProblem::kLink : PuzzleProblem<4>::kLink);
+            }
             a.outs[i] = o;
             if (a.serving) a.states[i] = st;
         }
         __syncthreads();
     }
+}
+
+// A deferred serving walk: one request's chain into out[0 .. cap), its
+// length into out[cap].
+__global__ void k_serve_walk(const Slot *part, uint32_t goal_slot, unsigned long long *out, uint64_t cap, int link) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) out[cap] = walk_chain(part, goal_slot, out, cap, link);
 }
 
 __device__ void clear_partition_team(Slot *tab, uint64_t slots, uint32_t rank, uint32_t nranks) {
@@ -290,9 +310,13 @@ __global__ void __launch_bounds__(512, 1) k_batch_cluster(BatchArgs a) {
             o.t_end = globaltimer_ns();
             const uint32_t pend = ldcg_u32(&st->error);
             if (o.status == ST_RUNNING && pend) o.status = pend;
-            if (o.status == ST_OK)
-                o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap,
-                                        d.kind == UASTAR_KIND_GRID ? GridProblem::kLink : PuzzleProblem<4>::kLink);
+            if (o.status == ST_OK) {
+                if (a.walk_inline && path_cells(d.kind, o.goal_best) > a.walk_inline)
+                    o.path_len = kWalkDeferred;  // walked after the quantum (the CTA kernel's note)
+                else
+                    o.path_len = walk_chain(tab, o.goal_slot, a.keys + d.key_off, d.key_cap,
+                                            d.kind == UASTAR_KIND_GRID ? GridProblem::kLink : PuzzleProblem<4>::kLink);
+            }
             a.outs[i] = o;
         }
         team.sync();
@@ -1088,6 +1112,16 @@ struct ServeSlot {
     uint64_t tab_off = 0, tab_n = 0, bm_off = 0, bm_n = 0, heap_off = 0, heap_n = 0;
 };
 
+// A solved request whose path is being walked after its quantum: its
+// partition stays allocated until the walk's keys are on the host.
+struct ServeWalk {
+    ServeReq req;
+    InstOut o{};
+    uint64_t tab_off = 0, tab_n = 0;
+    uint64_t ring_off = 0, n = 0;  // n path cells at ring_off (and their count after them)
+    cudaEvent_t ev = nullptr;
+};
+
 // One kind of resident slot: single CTAs (puzzles, small grids) or 8-CTA
 // clusters (large grids, and requests that outgrew a CTA).  Each tier has its
 // own quantum kernel and stream and is relaunched as soon as its previous
@@ -1146,6 +1180,14 @@ struct ServeState {
     // device arenas shared by both tiers
     DevBuf tab, bitmaps, heaps;
     RangeAlloc tab_alloc, bm_alloc, heap_alloc;  // units: slots, 8-byte words, 16-byte heap units
+    // Deferred path walks (long paths), on their own stream after the
+    // quantum that solved them: a ring of key room on the device and in
+    // pinned host memory, used in the order the walks were issued.
+    cudaStream_t walk_stream = nullptr;
+    DevBuf walk_ring;
+    unsigned long long *h_walk_ring = nullptr;
+    uint64_t walk_ring_keys = 0;
+    std::deque<ServeWalk> walking;
 };
 
 static void serve_complete(ServeState *S, ServeReq &r, int32_t status) {
@@ -1290,6 +1332,9 @@ static BatchArgs serve_args(ServeState *S, ServeTier &t) {
     // finished request for its slice's end).
     const bool sliced = S->cfg.quantum_us >= 0;
     a.quantum_ns = sliced ? (uint64_t)(S->cfg.quantum_us > 0 ? S->cfg.quantum_us : 8000) * 1000ull : 0;
+    // paths beyond 1024 cells (~0.5 ms of pointer chase) are walked after
+    // the quantum, on the walk stream (serve_walk_issue)
+    a.walk_inline = 1024;
     a.budget = (uint64_t)(S->cfg.rounds_per_quantum > 0 ? S->cfg.rounds_per_quantum : sliced ? 65536 : 256);
     a.serving = 1;
     a.keys = t.d_keys.as<unsigned long long>();
@@ -1411,6 +1456,86 @@ static int32_t serve_finish_ok(ServeReq &r, const InstOut &o, const std::vector<
         uastar_validate_puzzle_moves(in.n, in.tiles, moves.data(), (int64_t)moves.size()) != UASTAR_OK)
         return UASTAR_CUDA_ERROR;
     return UASTAR_OK;
+}
+
+// Room for n keys in the walk ring, used first in, first out.
+static bool walk_ring_alloc(ServeState *S, uint64_t n, uint64_t *off) {
+    const uint64_t R = S->walk_ring_keys;
+    if (n > R) return false;
+    if (S->walking.empty()) {
+        *off = 0;
+        return true;
+    }
+    const uint64_t tail = S->walking.front().ring_off;
+    const uint64_t head = S->walking.back().ring_off + S->walking.back().n + 1;
+    if (head > tail) {  // in use: [tail, head)
+        if (head + n <= R) {
+            *off = head;
+            return true;
+        }
+        if (n <= tail) {  // wrap to the start
+            *off = 0;
+            return true;
+        }
+        return false;
+    }
+    if (head + n <= tail) {  // in use: [tail, R) and [0, head)
+        *off = head;
+        return true;
+    }
+    return false;
+}
+
+// Walk slot q's solved request (a path longer than the in-quantum limit)
+// on the walk stream behind the quantum that solved it, into the ring, and
+// copy the keys to the pinned ring; the request completes when they are on
+// the host (serve_walk_finish).  Its heap slice and bitmap are released now,
+// its partition then.  False: no ring room (the caller walks it now).
+static bool serve_walk_issue(ServeState *S, ServeTier &t, int q) {
+    const InstOut &o = t.outs[q];
+    ServeSlot &sl = t.slots[q];
+    const uint64_t n = path_cells(sl.req.inst.kind, o.goal_best);
+    uint64_t off = 0;
+    if (!walk_ring_alloc(S, n + 1, &off)) return false;
+    ServeWalk w;
+    if (cudaEventCreateWithFlags(&w.ev, cudaEventDisableTiming) != cudaSuccess) return false;
+    unsigned long long *d = S->walk_ring.as<unsigned long long>() + off;
+    cudaStreamWaitEvent(S->walk_stream, t.done, 0);
+    k_serve_walk<<<1, 32, 0, S->walk_stream>>>(
+        S->tab.as<Slot>() + sl.tab_off, o.goal_slot, d, n,
+        sl.req.inst.kind == UASTAR_KIND_GRID ? GridProblem::kLink : PuzzleProblem<4>::kLink);
+    S->eng->launches++;
+    cudaMemcpyAsync(S->h_walk_ring + off, d, (n + 1) * 8, cudaMemcpyDeviceToHost, S->walk_stream);
+    cudaEventRecord(w.ev, S->walk_stream);
+    if (cudaGetLastError() != cudaSuccess) {
+        S->loop_error = UASTAR_CUDA_ERROR;
+        cudaEventDestroy(w.ev);
+        return false;
+    }
+    w.o = o;
+    w.tab_off = sl.tab_off;
+    w.tab_n = sl.tab_n;
+    w.ring_off = off;
+    w.n = n;
+    if (sl.bm_n) S->bm_alloc.release(sl.bm_off, sl.bm_n);
+    S->heap_alloc.release(sl.heap_off, sl.heap_n);
+    w.req = std::move(sl.req);
+    S->walking.push_back(std::move(w));
+    return true;
+}
+
+// A deferred walk's keys are on the host: validate and complete.
+static void serve_walk_finish(ServeState *S, ServeWalk &w) {
+    const unsigned long long *h = S->h_walk_ring + w.ring_off;
+    const uint64_t len = h[w.n];
+    int32_t status = UASTAR_CUDA_ERROR;
+    if (len == w.n) {
+        std::vector<unsigned long long> keys(h, h + len);
+        status = serve_finish_ok(w.req, w.o, keys);
+    }
+    S->tab_alloc.release(w.tab_off, w.tab_n);
+    cudaEventDestroy(w.ev);
+    serve_complete(S, w.req, status);
 }
 
 // Move slot q's paused search (it passed grow_at) to a partition 4x larger:
@@ -1586,6 +1711,12 @@ static void serve_retire(ServeState *S, ServeTier &t, std::deque<ServeReq> &to_l
         r.acc.generated += (int64_t)o.generated;
         r.acc.rounds += (int64_t)o.rounds;
         int32_t status = (int32_t)o.status;
+        if (status == ST_OK && o.path_len == kWalkDeferred && serve_walk_issue(S, t, q)) {
+            t.descs[q].kind = 0;
+            sl = ServeSlot();
+            continue;
+        }
+        if (S->loop_error) return;
         if (status == ST_OK) {
             if (serve_path(S, t, q, keys) != cudaSuccess) {
                 S->loop_error = UASTAR_CUDA_ERROR;
@@ -1703,6 +1834,18 @@ static void serve_loop(ServeState *S) {
             serve_retire(S, t, to_large, spare);
         }
         if (S->loop_error) break;
+        // 2b. deferred walks whose keys are on the host complete
+        while (!S->walking.empty()) {
+            e = cudaEventQuery(S->walking.front().ev);
+            if (e == cudaErrorNotReady) break;
+            if (e != cudaSuccess) {
+                fail(e, "serve walk");
+                break;
+            }
+            serve_walk_finish(S, S->walking.front());
+            S->walking.pop_front();
+        }
+        if (S->loop_error) break;
         // 3. admission: promoted requests take cluster slots, then arrived
         //    requests take CTA slots in arrival order
         while (!to_large.empty()) {
@@ -1780,6 +1923,12 @@ static void serve_loop(ServeState *S) {
     }
     for (auto &t : S->tier)
         if (t.stream) cudaStreamSynchronize(t.stream);
+    // solved requests still being walked complete as solved
+    if (S->walk_stream) cudaStreamSynchronize(S->walk_stream);
+    while (!S->walking.empty()) {
+        serve_walk_finish(S, S->walking.front());
+        S->walking.pop_front();
+    }
     // drain: anything left is reported as cancelled
     for (auto &r : pending) serve_complete(S, r, UASTAR_CANCELLED);
     for (auto &r : to_large) serve_complete(S, r, UASTAR_CANCELLED);
@@ -1803,7 +1952,11 @@ static void serve_free(ServeState *S) {
         if (t.done) cudaEventDestroy(t.done);
         if (t.stream) cudaStreamDestroy(t.stream);
     }
-    for (DevBuf *b : {&S->tab, &S->bitmaps, &S->heaps}) b->release();
+    for (DevBuf *b : {&S->tab, &S->bitmaps, &S->heaps, &S->walk_ring}) b->release();
+    if (S->h_walk_ring) cudaFreeHost(S->h_walk_ring);
+    S->h_walk_ring = nullptr;
+    if (S->walk_stream) cudaStreamDestroy(S->walk_stream);
+    S->walk_stream = nullptr;
 }
 
 }  // namespace uastar
@@ -1887,6 +2040,11 @@ int32_t uastar_serve_start(uastar_engine *eng, const uastar_serve_config *cfg) {
     if ((e = S->tab.ensure(tab_slots * sizeof(Slot))) == cudaSuccess)
         e = S->bitmaps.ensure(bm_words * 8 + 64);
     if (e == cudaSuccess) e = S->heaps.ensure(S->heap_bytes);
+    // deferred walks: 4 M keys of ring (32 MB here and pinned on the host)
+    S->walk_ring_keys = 1ull << 22;
+    if (e == cudaSuccess) e = S->walk_ring.ensure(S->walk_ring_keys * 8);
+    if (e == cudaSuccess) e = cudaMallocHost(&S->h_walk_ring, S->walk_ring_keys * 8);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->walk_stream, cudaStreamNonBlocking);
     for (auto &t : S->tier) {
         if (e != cudaSuccess) break;
         const size_t ctas = (size_t)t.nslots * (t.large ? 8 : 1);
