@@ -1134,6 +1134,12 @@ struct ServeTier {
     std::vector<InstDesc> descs;
     std::vector<InstOut> outs;
     DevBuf d_descs, d_outs, d_states, d_hsize, d_cand, d_keys, d_walk, d_map;
+    // pinned mirrors of descs / outs for the launch's copies: with pageable
+    // memory the device-to-host copy of the outs would hold the host thread
+    // until the quantum ends, and the other tier could not be launched beside it
+    InstDesc *h_descs = nullptr;
+    InstOut *h_outs = nullptr;
+    int launched_n = 0;  // slots the quantum in flight covers
     uint64_t kcap = 0;  // path keys per slot (walked in the kernel)
     cudaStream_t stream = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr, done = nullptr;
@@ -1188,6 +1194,16 @@ struct ServeState {
     unsigned long long *h_walk_ring = nullptr;
     uint64_t walk_ring_keys = 0;
     std::deque<ServeWalk> walking;
+    // Pinned staging for bitmap uploads at admission (a copy from pageable
+    // memory may wait for the tier's running quantum): ranges in the order
+    // they were staged, each free again once its copy has run.
+    unsigned char *h_stage = nullptr;
+    uint64_t stage_bytes = 0;
+    struct Staged {
+        uint64_t off, n;
+        cudaEvent_t ev;
+    };
+    std::deque<Staged> staged;
 };
 
 static void serve_complete(ServeState *S, ServeReq &r, int32_t status) {
@@ -1220,6 +1236,42 @@ static void serve_release(ServeState *S, ServeSlot &sl) {
     S->tab_alloc.release(sl.tab_off, sl.tab_n);
     if (sl.bm_n) S->bm_alloc.release(sl.bm_off, sl.bm_n);
     S->heap_alloc.release(sl.heap_off, sl.heap_n);
+}
+
+// Copy n host bytes to dst on t's stream through the pinned staging ring
+// (a plain pageable copy where the ring has no room).
+static cudaError_t serve_upload(ServeState *S, ServeTier &t, void *dst, const void *src, uint64_t n) {
+    while (!S->staged.empty() && cudaEventQuery(S->staged.front().ev) == cudaSuccess) {
+        cudaEventDestroy(S->staged.front().ev);
+        S->staged.pop_front();
+    }
+    const uint64_t need = (n + 255) & ~255ull, R = S->stage_bytes;
+    uint64_t off = 0;
+    bool room = need <= R;
+    if (room && !S->staged.empty()) {
+        const uint64_t tail = S->staged.front().off, head = S->staged.back().off + S->staged.back().n;
+        if (head > tail) {  // in use: [tail, head)
+            if (head + need <= R)
+                off = head;
+            else if (need <= tail)
+                off = 0;  // wrap to the start
+            else
+                room = false;
+        } else {  // in use: [tail, R) and [0, head)
+            if (head + need <= tail)
+                off = head;
+            else
+                room = false;
+        }
+    }
+    cudaEvent_t ev = nullptr;
+    if (room && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) room = false;
+    if (!room) return cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, t.stream);
+    std::memcpy(S->h_stage + off, src, n);
+    cudaError_t e = cudaMemcpyAsync(dst, S->h_stage + off, n, cudaMemcpyHostToDevice, t.stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev, t.stream);
+    S->staged.push_back({off, need, ev});
+    return e;
 }
 
 // Try to place `r` in a free slot of tier `t`.  Returns 1 placed, 0 no room
@@ -1290,8 +1342,8 @@ static int serve_admit(ServeState *S, ServeTier &t, ServeReq &r) {
         d.ex = sl.req.inst.ex;
         d.ey = sl.req.inst.ey;
         d.bm_word = boff * 2;
-        if (cudaMemcpyAsync(S->bitmaps.as<uint64_t>() + boff, sl.req.words.data(), sl.req.words.size() * 8,
-                            cudaMemcpyHostToDevice, t.stream) != cudaSuccess)
+        if (serve_upload(S, t, S->bitmaps.as<uint64_t>() + boff, sl.req.words.data(), sl.req.words.size() * 8) !=
+            cudaSuccess)
             S->loop_error = UASTAR_CUDA_ERROR;
     } else {
         d.start_key = pack_board(d.n, sl.req.inst.tiles);
@@ -1346,7 +1398,8 @@ static BatchArgs serve_args(ServeState *S, ServeTier &t) {
 static cudaError_t serve_launch(ServeState *S, ServeTier &t) {
     cudaError_t e;
     const int n = t.extent();
-    if ((e = cudaMemcpyAsync(t.d_descs.p, t.descs.data(), n * sizeof(InstDesc), cudaMemcpyHostToDevice,
+    std::memcpy(t.h_descs, t.descs.data(), n * sizeof(InstDesc));
+    if ((e = cudaMemcpyAsync(t.d_descs.p, t.h_descs, n * sizeof(InstDesc), cudaMemcpyHostToDevice,
                              t.stream)) != cudaSuccess)
         return e;
     BatchArgs a = serve_args(S, t);
@@ -1372,7 +1425,8 @@ static cudaError_t serve_launch(ServeState *S, ServeTier &t) {
     S->eng->launches++;
     if (e != cudaSuccess) return e;
     cudaEventRecord(t.e1, t.stream);
-    if ((e = cudaMemcpyAsync(t.outs.data(), t.d_outs.p, n * sizeof(InstOut), cudaMemcpyDeviceToHost,
+    t.launched_n = n;
+    if ((e = cudaMemcpyAsync(t.h_outs, t.d_outs.p, n * sizeof(InstOut), cudaMemcpyDeviceToHost,
                              t.stream)) != cudaSuccess)
         return e;
     if ((e = cudaEventRecord(t.done, t.stream)) != cudaSuccess) return e;
@@ -1679,6 +1733,7 @@ static bool serve_migrate(ServeState *S, int q) {
 // which a cluster would not shorten.
 static void serve_retire(ServeState *S, ServeTier &t, std::deque<ServeReq> &to_large, bool spare) {
     ServeTier &large = S->tier[1];
+    std::memcpy(t.outs.data(), t.h_outs, (size_t)t.launched_n * sizeof(InstOut));
     for (const auto &r : t.release_after) S->tab_alloc.release(r.first, r.second);
     t.release_after.clear();
     float ms = 0;
@@ -1895,11 +1950,15 @@ static void serve_loop(ServeState *S) {
                                                (double)S->bm_alloc.used() * 8 + (double)S->heap_alloc.used() * 16) /
                                                   1e9);
         if (S->loop_error) break;
-        // 4. launch every idle tier that has work: the cluster tier first
-        //    (its CTAs need whole GPCs)
-        for (int ti = 1; ti >= 0; --ti) {
+        // 4. launch the tiers that have work, together and the cluster tier
+        //    first, once neither is in flight: a cluster's 8 CTAs need room
+        //    in one GPC at once, which a CTA-tier launch spread over every SM
+        //    does not leave, so launched apart the two kernels would take
+        //    turns on the GPU instead of sharing it
+        const bool idle = !small.inflight && !large.inflight;
+        for (int ti = 1; ti >= 0 && idle; --ti) {
             ServeTier &t = S->tier[ti];
-            if (t.inflight || !t.nslots || !t.resident()) continue;
+            if (!t.nslots || !t.resident()) continue;
             if ((e = serve_launch(S, t)) != cudaSuccess) {
                 fail(e, "serve launch");
                 break;
@@ -1951,10 +2010,18 @@ static void serve_free(ServeState *S) {
         if (t.e1) cudaEventDestroy(t.e1);
         if (t.done) cudaEventDestroy(t.done);
         if (t.stream) cudaStreamDestroy(t.stream);
+        if (t.h_descs) cudaFreeHost(t.h_descs);
+        if (t.h_outs) cudaFreeHost(t.h_outs);
+        t.h_descs = nullptr;
+        t.h_outs = nullptr;
     }
     for (DevBuf *b : {&S->tab, &S->bitmaps, &S->heaps, &S->walk_ring}) b->release();
     if (S->h_walk_ring) cudaFreeHost(S->h_walk_ring);
     S->h_walk_ring = nullptr;
+    for (auto &st : S->staged) cudaEventDestroy(st.ev);
+    S->staged.clear();
+    if (S->h_stage) cudaFreeHost(S->h_stage);
+    S->h_stage = nullptr;
     if (S->walk_stream) cudaStreamDestroy(S->walk_stream);
     S->walk_stream = nullptr;
 }
@@ -2045,6 +2112,9 @@ int32_t uastar_serve_start(uastar_engine *eng, const uastar_serve_config *cfg) {
     if (e == cudaSuccess) e = S->walk_ring.ensure(S->walk_ring_keys * 8);
     if (e == cudaSuccess) e = cudaMallocHost(&S->h_walk_ring, S->walk_ring_keys * 8);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->walk_stream, cudaStreamNonBlocking);
+    // bitmap uploads: 128 MB of pinned staging
+    S->stage_bytes = 128ull << 20;
+    if (e == cudaSuccess) e = cudaMallocHost(&S->h_stage, S->stage_bytes);
     for (auto &t : S->tier) {
         if (e != cudaSuccess) break;
         const size_t ctas = (size_t)t.nslots * (t.large ? 8 : 1);
@@ -2052,6 +2122,9 @@ int32_t uastar_serve_start(uastar_engine *eng, const uastar_serve_config *cfg) {
         t.descs.assign(t.nslots, InstDesc());
         std::memset(t.descs.data(), 0, t.descs.size() * sizeof(InstDesc));
         t.outs.assign(t.nslots, InstOut());
+        if ((e = cudaMallocHost(&t.h_descs, std::max(1, t.nslots) * sizeof(InstDesc))) != cudaSuccess ||
+            (e = cudaMallocHost(&t.h_outs, std::max(1, t.nslots) * sizeof(InstOut))) != cudaSuccess)
+            break;
         if (!t.nslots) continue;
         t.kcap = 65600;  // path keys per slot (2 (H + W) + 64 for grids up to 16384 x 16384)
         if ((e = t.d_keys.ensure((size_t)t.nslots * t.kcap * 8)) != cudaSuccess ||
