@@ -942,8 +942,13 @@ int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int
                 stats->generated += gr.generated;
             }
         } else {
+            // the plain engine starts this puzzle's table at 2^26 slots: it
+            // filled a cluster's partition or ran out of its round budget
+            // there, and every 4x growth on the way up pauses the search
             uastar_puzzle_result pr;
+            eng->puzzle_log2_start = 26;
             rc = uastar_puzzle_solve(eng, in.n, in.tiles, &pr);
+            eng->puzzle_log2_start = 0;
             r.status = pr.status;
             r.steps = pr.steps;
             r.expanded += pr.expanded;

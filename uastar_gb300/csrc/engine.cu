@@ -630,7 +630,8 @@ int32_t puzzle_solve_n(uastar_engine *eng, const uint8_t *tiles, PlainOut *po) {
     prob.pdb = eng->pdb[N].as<uint8_t>();
     prob.start = pack_board(N, tiles);
     prob.goal = PuzzleProblem<N>::goal_key();
-    return run_plain(eng, prob, N == 3 ? 20 : 22, N == 3 ? 1024 : 16383, po);
+    const int log2_start = eng->puzzle_log2_start > 0 ? eng->puzzle_log2_start : (N == 3 ? 20 : 22);
+    return run_plain(eng, prob, log2_start, N == 3 ? 1024 : 16383, po);
 }
 
 // 5x5: 16-byte keys (PuzzleProblem<5>)

@@ -87,6 +87,10 @@ struct uastar_engine {
     // plain engine buffers
     uastar::DevBuf tab, heaps, heap_size, cand, team, walk, bitmap;
     uastar::DevBuf tab_next, grow_map;  // table growth of a paused search
+    // first table of a 3x3 / 4x4 plain solve, log2 slots (0: 2^20 / 2^22);
+    // the batched engine raises it for the puzzles it escalates, which have
+    // already filled a cluster's partition or round budget
+    int puzzle_log2_start = 0;
     uastar::DevBuf sortb;               // per-round successor sort (dedup = 1), uastar_sort_keys
     uastar::DevBuf ida;                 // memory-bounded mode: IDA* roots and pass state
     // launch-configuration queries of the plain engine, made once per shape:
