@@ -260,8 +260,8 @@ typedef struct {
 typedef struct {
     int32_t threads_per_instance; /* CTA size per instance (0 -> 256) */
     int32_t threads_per_heap;     /* heaps per instance = threads_per_instance / this (0 -> 4) */
-    int32_t heap_capacity;        /* entries per heap (0 -> autotuned) */
-    double load_factor;           /* target dedup-partition load (0 -> autotuned) */
+    int32_t heap_capacity;        /* entries per heap (0 -> 4095; uastar_autotune picks one) */
+    double load_factor;           /* target dedup-partition load (0 -> 0.5; uastar_autotune picks one) */
     int32_t ctas;                 /* persistent CTAs (0 -> all SMs x occupancy) */
     int32_t use_graph;            /* launch through a captured CUDA graph (default 1) */
     int32_t tier1_rounds;         /* round budget of a single-CTA team (0 -> 2048) */
@@ -284,13 +284,15 @@ typedef struct {
     int64_t partition_bytes;  /* device bytes of all dedup partitions */
 } uastar_batch_stats;
 
-/* Solve `count` instances of mixed kinds in one persistent launch; each CTA
- * takes instances from a device work queue and runs GA* on it with its own
- * heap slice and dedup partition.  Instances whose partition or heaps
- * overflow are re-run in a second wave with 8x the partition (4x the heaps);
- * those that overflow again are escalated to the plain engine.  No
- * counterpart in the reference (spec extension of
- * GPUPathwaySolver/GPUPuzzleSolver). */
+/* Solve `count` instances of mixed kinds with persistent launches: in the
+ * first wave each CTA takes instances from a device work queue and runs GA*
+ * on one with its own heap slice and dedup partition, under a round budget
+ * (tier1_rounds); grids above 2048^2 and the instances that ran out of rounds
+ * or space go to a second wave of 8-CTA cluster teams with 16x the
+ * partition (puzzles under tier2_puzzle_rounds), and what fails there is
+ * solved by the plain engine, one instance at a time.  No counterpart in the
+ * reference, which solves one instance per process through
+ * GPUPathwaySolver / GPUPuzzleSolver. */
 int32_t uastar_batch_solve(uastar_engine *eng, const uastar_instance *insts, int32_t count,
                            const uastar_batch_config *cfg, uastar_instance_result *results,
                            uastar_batch_stats *stats);
