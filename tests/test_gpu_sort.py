@@ -74,7 +74,7 @@ def test_sorted_golden_small_grids():
 
 
 def test_sorted_grid_1000_equals_default_mode(seng):
-    """C1 in both modes: the reference's step counts, and the table grows in
+    """The 1000x1000 grid (30 % blocked) in both modes: the reference's step counts, and the table grows in
     place at least once from its 2^20-slot start in the sorted mode too."""
     c = golden("grid_c1.json")
     w = case_words(c)
